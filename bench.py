@@ -1,0 +1,403 @@
+#!/usr/bin/env python3
+"""Headline benchmark: box2d3r (49-point 7x7) on a 8192 x 8192 float64 grid.
+
+One "step" is one stencil time step (one sweep of the 49-point kernel over
+the whole grid). Default: 1000 steps, the workload's full length.
+
+  value    GStencil/s of the split-precision path (FP32 hi+lo grids, exact BF16
+           slices on tensor cores), device-resident, K steps timed with CUDA
+           events on the launching stream. The FP64 path (same GPU) is timed
+           the same way and reported under "fp64"; the split result's error
+           against the FP64 path is stated under "err".
+  e2e      the same K steps through the reference-shaped C ABI with HOST
+           buffers (cs_gpu_box_2d3r for FP64, cs_run_host for split): device
+           allocation, host->device copy, K sweeps, device->host copy inside
+           the timed region.
+  roofline the dominant kernel's achieved rate over its measured peak.
+  cpu_baseline  the CPU oracle (OpenMP C restatement of the reference's
+           naive stencil) on the host cores, on a bounded sample.
+
+--impl reference runs the reference's CPU stencil path (the oracle port, all
+host cores) on the same workload and prints its own line.
+Under torchrun with N ranks each rank runs an independent replica (the
+reference has no multi-GPU path; replicas only), value = N * work / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M = N = 8192
+SHAPE = "box2d3r"
+TAPS = 49
+GRID_SEED, WEIGHT_SEED = 1, 2
+METRIC = "GStencil/s (split-prec vs FP64, same GB300, stated err); served p50/p99 latency"
+WORKLOAD = "box2d3r 8192x8192 float64, 49 seeded weights normalised to sum 1, zero halo radius 3"
+FP64_PEAK_TFLOPS = 1.05  # measured DMMA/DFMA ceiling on GB300, profiles/fp64_pipe_peak_gb300.md
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_key}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self._proc:
+            time.sleep(0.15)
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def seeded_inputs():
+    from oracle import cs_oracle as O  # the shared SplitMix64 restatement
+    x = O.splitmix_uniform(M * N, GRID_SEED).reshape(M, N)
+    w = O.seeded_weights(TAPS, WEIGHT_SEED)
+    return x, w
+
+
+def oracle_sample(x, w, rows, steps, threads=None):
+    """Times the CPU oracle on a rows x N slab for `steps` sweeps; returns
+    (seconds, points*steps)."""
+    from oracle import cs_oracle as O
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    ld = N + 8
+    g = np.zeros((rows + 6, ld))
+    g[3:rows + 3, 4:N + 4] = x[:rows]
+    t0 = time.perf_counter()
+    O.run_2d(g, w, 3, rows, N, 3, 4, steps)
+    return time.perf_counter() - t0, rows * N * steps
+
+
+# ----------------------------------------------------------------- reference
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    from oracle import cs_oracle as O
+    O.build()
+    x, w = seeded_inputs()
+    cores = os.cpu_count() or 1
+    # Calibrate a slab so one step is ~max(0.05, budget/(K+W)) seconds.
+    t, _ = oracle_sample(x, w, 256, 1)
+    per_row = t / 256
+    budget = 90.0
+    rows = int(max(64, min(M, budget / max(1, args.steps + args.warmup) / per_row)))
+    for _ in range(args.warmup):
+        oracle_sample(x, w, rows, 1)
+    tot_t, tot_pts = 0.0, 0
+    for _ in range(args.steps):
+        t, pts = oracle_sample(x, w, rows, 1)
+        tot_t += t
+        tot_pts += pts
+    val = tot_pts / tot_t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "GStencil/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (SplitMix64 seeded)",
+        "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": args.steps,
+                   "sample": f"each step = one sweep over a {rows} x {N} slab"},
+        "cpu_baseline": {"value": round(val, 4), "unit": "GStencil/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} sweeps of a {rows}x{N} slab, OpenMP on {cores} threads"},
+        "e2e": {"value": round(val, 4), "unit": "GStencil/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------- ours
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    args.warmup = max(3, args.warmup)
+
+    import torch
+    import convstencil_gb300 as cs
+
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+
+    x, w = seeded_inputs()
+    peaks, peak_src = load_peaks()
+    K, W = args.steps, args.warmup
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed_device_run(plan, a, b, steps, sampler=None):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        l0 = cs.kernel_launch_count()
+        ev0.record(stream)
+        in_b = plan.run(a, b, steps, stream=stream)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        launches = cs.kernel_launch_count() - l0
+        return ev0.elapsed_time(ev1) / 1e3, in_b, launches
+
+    def kernel_avg_seconds(plan, a, b, reps=5):
+        """Average duration of one sweep kernel, CUDA events on its stream."""
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        plan.run(a, b, reps, stream=stream)
+        ev1.record(stream)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / 1e3 / reps
+
+    results = {}
+    # ---------------- FP64 path
+    p64 = cs.Plan(SHAPE, (M, N), w)
+    host = p64.pack(x)
+    a64 = torch.from_numpy(host).to(dev)
+    b64 = torch.zeros_like(a64)
+    if not args.no_fp64:
+        p64.run(a64, b64, W, stream=stream)  # warm-up sweeps (also runs the tuner)
+        torch.cuda.synchronize()
+        a64.copy_(torch.from_numpy(host))
+        b64.zero_()
+        with ClockSampler(local) as cl64:
+            t64, in_b64, l64 = timed_device_run(p64, a64, b64, K)
+        t64 = max_over_ranks(t64)
+        res64 = (b64 if in_b64 else a64)
+        results["fp64"] = {"seconds": t64, "launches": l64, "clocks": cl64.summary()}
+        k64 = kernel_avg_seconds(p64, a64, b64)
+        results["fp64"]["kernel_s"] = k64
+
+    # ---------------- split path
+    split_ok = True
+    try:
+        psp = cs.Plan(SHAPE, (M, N), w, precision=cs.Precision.SPLIT)
+    except cs.ConvStencilError:
+        split_ok = False
+    if split_ok:
+        raw = torch.from_numpy(host).to(dev)
+        sa = torch.zeros(psp.elements * 2, dtype=torch.float32, device=dev)
+        sb = torch.zeros_like(sa)
+        psp.split_from_fp64(raw, sa, stream=stream)
+        s0 = sa.clone()
+        psp.run(sa, sb, W, stream=stream)
+        torch.cuda.synchronize()
+        sa.copy_(s0)
+        sb.zero_()
+        with ClockSampler(local) as clsp:
+            tsp, in_bsp, lsp = timed_device_run(psp, sa, sb, K)
+        tsp = max_over_ranks(tsp)
+        out_sp = torch.zeros(psp.elements, dtype=torch.float64, device=dev)
+        psp.split_to_fp64(sb if in_bsp else sa, out_sp, stream=stream)
+        torch.cuda.synchronize()
+        results["split"] = {"seconds": tsp, "launches": lsp, "clocks": clsp.summary()}
+        results["split"]["kernel_s"] = kernel_avg_seconds(psp, sa, sb)
+        if "fp64" in results:
+            ref = res64
+            d = (out_sp - ref).abs()
+            scale = ref.abs().max()
+            den = torch.clamp(ref.abs(), min=float(scale) * 1e-3)
+            results["split"]["err_vs_fp64"] = {
+                "max_rel": float((d / den).max()), "mean_rel": float((d / den).mean()),
+                "normwise": float(d.max() / scale)}
+        del raw, s0
+
+    headline = "split" if "split" in results else "fp64"
+    hr = results[headline]
+    pts = float(M) * N
+    value = world * pts * K / hr["seconds"] / 1e9
+
+    # ---------------- roofline of the dominant kernel
+    if headline == "fp64":
+        flops = 2.0 * TAPS * pts
+        ach = flops / hr["kernel_s"] / 1e12
+        roof = {"bound": "tensor", "achieved": round(ach, 4), "peak": FP64_PEAK_TFLOPS,
+                "unit": "TFLOP/s", "frac": round(ach / FP64_PEAK_TFLOPS, 4),
+                "traffic": profile_traffic("fp64_box2d3r_sweep"),
+                "kernel": "k2d_fma<3,dense>", "peak_source": "FP64 pipe microbenchmark (DFMA=DMMA pipe)",
+                "algorithmic": f"{2 * TAPS} FLOP/pt x {M}x{N} pts per launch"}
+    else:
+        byts = 16.0 * pts
+        ach = byts / hr["kernel_s"] / 1e9
+        pk = float(peaks["hbm_gbs"])
+        roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": pk, "unit": "GB/s",
+                "frac": round(ach / pk, 4), "traffic": profile_traffic("split_box2d3r_sweep"),
+                "kernel": "split sweep", "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic": f"16 B/pt (8 B read + 8 B write) x {M}x{N} pts per launch"}
+
+    # ---------------- e2e through the reference-shaped C ABI (host buffers)
+    e2e = None
+    if not args.no_e2e:
+        pin_in = torch.from_numpy(host).pin_memory()
+        pin_out = torch.empty_like(pin_in).pin_memory()
+        L = cs.lib()
+        dp = ctypes.POINTER(ctypes.c_double)
+        pin_p = ctypes.cast(pin_in.data_ptr(), dp)
+        out_p = ctypes.cast(pin_out.data_ptr(), dp)
+        wp = np.ascontiguousarray(w)
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if headline == "split":
+            cs.check(L.cs_run_host(psp._h, pin_p, out_p, K))
+        else:
+            # cs_gpu_box_2d3r takes the reference layout (m+6) x (n+8)
+            ref_in = np.zeros((M + 6, N + 8))
+            ref_in[3:M + 3, 4:N + 4] = x
+            ref_pin = torch.from_numpy(ref_in.reshape(-1)).pin_memory()
+            ref_out = torch.empty_like(ref_pin).pin_memory()
+            t0 = time.perf_counter()
+            cs.check(L.cs_gpu_box_2d3r(ctypes.cast(ref_pin.data_ptr(), dp),
+                                       ctypes.cast(ref_out.data_ptr(), dp),
+                                       wp.ctypes.data_as(dp), K, M, N))
+        te = time.perf_counter() - t0
+        te = max_over_ranks(te)
+        barrier()
+        gbytes = float(host.nbytes)
+        e2e = {"value": round(world * pts * K / te / 1e9, 4), "unit": "GStencil/s",
+               "h2d_bytes_per_step": round(gbytes / K, 1), "d2h_bytes_per_step": round(gbytes / K, 1),
+               "note": f"one {gbytes / 1e6:.0f} MB host->device and device->host copy per {K}-step run "
+                       "(the reference wrapper's contract), pinned host buffers, allocation included"}
+
+    # ---------------- CPU oracle baseline (bounded sample)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import cs_oracle as O
+        O.build()
+        cores = os.cpu_count() or 1
+        t, _ = oracle_sample(x, w, 256, 1)
+        rows = int(max(64, min(M, 15.0 / (t / 256))))
+        t, work = oracle_sample(x, w, rows, 1)
+        cpu = {"value": round(work / t / 1e9, 4), "unit": "GStencil/s", "cores": cores, "kind": "port",
+               "sample": f"1 sweep of a {rows}x{N} slab of the same grid (OpenMP C oracle)"}
+
+    if rank != 0:
+        return 0
+    clocks = hr["clocks"]
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "GStencil/s", "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": round(hr["seconds"] / K * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32x2 split (bf16 slices, f32 accum)" if headline == "split" else "f64",
+        "data": "synthetic (SplitMix64 seeded grid and weights)",
+        "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": K, "precision": headline,
+                   "l2": "inputs larger than L2 (537 MB per grid vs 129 MB L2)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
+        "gpu_launches": hr["launches"], "clocks": clocks,
+    }
+    if "fp64" in results:
+        r = results["fp64"]
+        line["fp64"] = {"value": round(world * pts * K / r["seconds"] / 1e9, 4), "unit": "GStencil/s",
+                        "ms_per_step": round(r["seconds"] / K * 1e3, 4),
+                        "kernel_ms": round(r["kernel_s"] * 1e3, 4), "launches": r["launches"],
+                        "clocks": r["clocks"]}
+    if "split" in results and "err_vs_fp64" in results["split"]:
+        line["err"] = results["split"]["err_vs_fp64"]
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,746 @@
+// cs_api.cu — host side of libconvstencil_gb300: plans, layouts, weight
+// algebra, the sweep loop, the tuner, and the reference-shaped wrappers.
+//
+// The reference's host wrappers (src/2d/gpu.cu:245-425, src/1d/gpu_1r.cu:227-302,
+// src/1d/gpu_2r.cu:85-159, src/3d/gpu_box.cu:446-536, src/3d/gpu_star.cu:238-332)
+// build B matrices and lookup tables, copy one grid in, ping-pong `times`
+// launches and copy the result out. Here the weights go to the kernels as
+// parameters (no __constant__ symbol, so plans are reentrant and independent
+// streams can run different stencils at once), no lookup tables exist (the
+// kernels index their tiles directly), and every failure is a status code.
+#include "../../include/convstencil.h"
+#include "cs_internal.h"
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <tuple>
+
+namespace cs {
+
+static std::atomic<long long> g_launches{0};
+void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+}  // namespace cs
+
+using cs::GridView;
+using cs::Weights;
+
+namespace {
+
+thread_local std::string t_err;
+thread_local double t_loop_seconds = 0.0;
+std::atomic<int> g_verbose{0};
+
+cs_status fail(cs_status s, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return s;
+}
+
+cs_status cuda_fail(cudaError_t e, const char *what)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return fail(CS_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return fail(CS_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+    return fail(CS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CS_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
+    } while (0)
+
+// Per-shape facts. Fused parameters and steps per fused sweep follow the
+// reference CLIs and wrappers: src/1d/main.cu:103-151, src/2d/main.cu:183-303,
+// src/3d/main.cu:526-567, src/3d/gpu_star.cu:30-56.
+struct ShapeInfo {
+    int dims, base_r, n_base, fused_r, n_fused, fused_steps;
+    const char *name;
+};
+const ShapeInfo kShapes[8] = {
+    {1, 1, 3, 3, 7, 3, "1d1r"},      {1, 2, 5, 4, 9, 2, "1d2r"},
+    {2, 1, 5, 3, 49, 3, "star2d1r"}, {2, 1, 9, 3, 49, 3, "box2d1r"},
+    {2, 3, 13, 3, 49, 1, "star2d3r"}, {2, 3, 49, 3, 49, 1, "box2d3r"},
+    {3, 1, 7, 3, 44, 3, "star3d1r"}, {3, 1, 27, 3, 196, 3, "box3d1r"},
+};
+
+int ipow(int b, int e)
+{
+    int r = 1;
+    while (e--) r *= b;
+    return r;
+}
+
+// Expand a shape's parameters to a dense (2r+1)^dims row-major kernel.
+bool expand_weights(cs_shape shape, cs_semantics sem, const double *p, Weights &w, int &radius)
+{
+    const ShapeInfo &si = kShapes[shape];
+    memset(w.v, 0, sizeof w.v);
+    if (sem == CS_SEM_STEP) {
+        radius = si.base_r;
+        switch (shape) {
+        case CS_SHAPE_STAR2D1R: {  // N, W, C, E, S at 3x3 cells 1,3,4,5,7 (src/2d/main.cu:211-217)
+            const int cell[5] = {1, 3, 4, 5, 7};
+            for (int i = 0; i < 5; ++i) w.v[cell[i]] = p[i];
+            return true;
+        }
+        case CS_SHAPE_STAR2D3R: {  // row-major cells of the radius-3 cross
+            int t = 0;
+            for (int i = 0; i < 7; ++i)
+                for (int j = 0; j < 7; ++j)
+                    if (i == 3 || j == 3) w.v[i * 7 + j] = p[t++];
+            return true;
+        }
+        case CS_SHAPE_STAR3D1R: {  // z-1, y-1, x-1, C, x+1, y+1, z+1 (src/3d/main.cu:557-565)
+            const int cell[7] = {4, 10, 12, 13, 14, 16, 22};
+            for (int i = 0; i < 7; ++i) w.v[cell[i]] = p[i];
+            return true;
+        }
+        default:
+            for (int i = 0; i < si.n_base; ++i) w.v[i] = p[i];
+            return true;
+        }
+    }
+    radius = si.fused_r;
+    if (shape == CS_SHAPE_BOX3D1R) {
+        // 4 planes of 49; plane q serves dz = +-(3-q) (src/3d/gpu_box.cu:450-468).
+        for (int a = 0; a < 7; ++a) {
+            const int q = 3 - std::abs(a - 3);
+            for (int t = 0; t < 49; ++t) w.v[a * 49 + t] = p[q * 49 + t];
+        }
+        return true;
+    }
+    if (shape == CS_SHAPE_STAR3D1R) {
+        // Plane |dz| holds the row-major cells of |dy|+|dx| <= 3-|dz|, blocks at
+        // 0, 1, 6, 19 (src/3d/main.cu:42-113, src/3d/gpu_star.cu:30-56).
+        const int base[4] = {0, 1, 6, 19};
+        for (int a = 0; a < 7; ++a) {
+            const int rho = 3 - std::abs(a - 3);
+            int t = base[rho];
+            for (int i = 0; i < 7; ++i)
+                for (int j = 0; j < 7; ++j)
+                    if (std::abs(i - 3) + std::abs(j - 3) <= rho) w.v[(a * 7 + i) * 7 + j] = p[t++];
+        }
+        return true;
+    }
+    for (int i = 0; i < si.n_fused; ++i) w.v[i] = p[i];
+    return true;
+}
+
+// Smallest tap pattern covering the non-zero weights.
+int classify(const Weights &w, int dims, int r)
+{
+    if (dims == 1) return cs::PAT_DENSE;
+    const int k = 2 * r + 1;
+    bool star = true, diamond = true;
+    const int n = ipow(k, dims);
+    for (int t = 0; t < n; ++t) {
+        if (w.v[t] == 0.0) continue;
+        int c[3] = {0, 0, 0}, rem = t;
+        for (int d = dims - 1; d >= 0; --d) {
+            c[d] = rem % k - r;
+            rem /= k;
+        }
+        int nz = 0, l1 = 0;
+        for (int d = 0; d < dims; ++d) {
+            nz += c[d] != 0;
+            l1 += std::abs(c[d]);
+        }
+        if (nz > 1) star = false;
+        if (l1 > r) diamond = false;
+    }
+    if (star) return cs::PAT_STAR;
+    if (diamond) return r == 1 ? cs::PAT_STAR : cs::PAT_DIAMOND;
+    return cs::PAT_DENSE;
+}
+
+long long round_up(long long v, long long a) { return (v + a - 1) / a * a; }
+
+void native_layout(int dims, int r, const long long *ext, cs_layout &L)
+{
+    memset(&L, 0, sizeof L);
+    L.dims = dims;
+    L.halo = r;
+    const long long x0 = round_up(r, 2);  // interior rows start 16-byte aligned
+    if (dims == 1) {
+        L.extent[0] = ext[0];
+        L.pitch[0] = 1;
+        L.origin = x0;
+        L.elements = round_up(x0 + ext[0] + r, 2);
+    } else if (dims == 2) {
+        L.extent[0] = ext[0];
+        L.extent[1] = ext[1];
+        L.pitch[1] = 1;
+        L.pitch[0] = round_up(x0 + ext[1] + r, 2);
+        L.origin = r * L.pitch[0] + x0;
+        L.elements = (ext[0] + 2 * r) * L.pitch[0];
+    } else {
+        for (int d = 0; d < 3; ++d) L.extent[d] = ext[d];
+        L.pitch[2] = 1;
+        L.pitch[1] = round_up(x0 + ext[2] + r, 2);
+        L.pitch[0] = L.pitch[1] * (ext[1] + 2 * r);
+        L.origin = r * L.pitch[0] + r * L.pitch[1] + x0;
+        L.elements = (ext[0] + 2 * r) * L.pitch[0];
+    }
+    L.bytes = (size_t)L.elements * sizeof(double);
+}
+
+// The tuner's memory: which algorithm won for a (dims, radius, pattern,
+// precision, log2 size) class. Process-wide, guarded by a mutex.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, int> g_tune;
+
+}  // namespace
+
+struct cs_plan {
+    cs_shape shape;
+    cs_semantics sem;
+    cs_precision prec;
+    int dims, radius, pattern, steps_per_sweep;
+    Weights w;
+    cs_layout layout;
+    GridView view;
+    int algo = CS_ALGO_AUTO;
+    int split_levels = 5;
+    long long reanchor = 100;
+    int time_block = 0;
+};
+
+namespace {
+
+bool fp64_mma_ok(const cs_plan *p)
+{
+    return p->prec == CS_PREC_FP64 && p->dims == 2 && p->radius == 3 &&
+           p->pattern == cs::PAT_DENSE;
+}
+
+cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *out_base,
+                         cudaStream_t st)
+{
+    const long long off = p->layout.origin;
+    if (p->prec == CS_PREC_FP64) {
+        const double *in = (const double *)in_base + off;
+        double *out = (double *)out_base + off;
+        if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(p->view, p->w, in, out, st);
+        return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st);
+    }
+    const float2 *in = (const float2 *)in_base + off;
+    float2 *out = (float2 *)out_base + off;
+    return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, p->split_levels, in, out,
+                                  st);
+}
+
+int size_class(const cs_plan *p)
+{
+    long long pts = 1;
+    for (int d = 0; d < p->dims; ++d) pts *= p->view.ext[d];
+    int c = 0;
+    while (pts > 1) {
+        pts >>= 2;
+        ++c;
+    }
+    return c;
+}
+
+// Picks the algorithm for a plan. With CS_ALGO_AUTO and more than one
+// candidate, the first sweep of the first run is timed once per candidate
+// (every candidate computes the same sweep a -> b, so the extra work changes
+// no result) and the winner is remembered for plans of the same class.
+cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *out)
+{
+    if (p->prec == CS_PREC_SPLIT) {
+        *out = CS_ALGO_SPLIT_MMA;
+        return CS_OK;
+    }
+    if (p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) {
+        *out = CS_ALGO_FP64_MMA;
+        return CS_OK;
+    }
+    if (p->algo != CS_ALGO_AUTO || !fp64_mma_ok(p)) {
+        *out = CS_ALGO_FP64_FMA;
+        return CS_OK;
+    }
+    auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            *out = it->second;
+            return CS_OK;
+        }
+    }
+    const int cand[2] = {CS_ALGO_FP64_FMA, CS_ALGO_FP64_MMA};
+    float best_ms = 1e30f;
+    int best = CS_ALGO_FP64_FMA;
+    cudaEvent_t e0, e1;
+    CS_CUDA(cudaEventCreate(&e0));
+    CS_CUDA(cudaEventCreate(&e1));
+    for (int rep = 0; rep < 2; ++rep) {  // rep 0 warms up
+        for (int c : cand) {
+            CS_CUDA(cudaEventRecord(e0, st));
+            CS_CUDA(launch_sweep(p, c, a, b, st));
+            CS_CUDA(cudaEventRecord(e1, st));
+            CS_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep == 1 && ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = best;
+    }
+    *out = best;
+    return CS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+CS_API const char *cs_status_string(cs_status s)
+{
+    switch (s) {
+    case CS_OK: return "ok";
+    case CS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case CS_ERR_UNSUPPORTED: return "unsupported";
+    case CS_ERR_CUDA: return "CUDA error";
+    case CS_ERR_OUT_OF_MEMORY: return "out of memory";
+    case CS_ERR_TIMEOUT: return "timeout";
+    case CS_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+CS_API const char *cs_last_error(void) { return t_err.c_str(); }
+CS_API void cs_set_verbose(int on) { g_verbose.store(on); }
+CS_API double cs_last_loop_seconds(void) { return t_loop_seconds; }
+CS_API long long cs_kernel_launch_count(void) { return cs::g_launches.load(); }
+CS_API const char *cs_version(void) { return "convstencil_gb300 0.1 (sm_103a)"; }
+
+CS_API cs_status cs_plan_create(cs_plan **out, cs_shape shape, cs_semantics sem, cs_precision prec,
+                                const long long *extent, const double *weights, int n_weights,
+                                const cs_layout *layout)
+{
+    if (!out) return fail(CS_ERR_INVALID_ARGUMENT, "plan pointer is NULL");
+    *out = nullptr;
+    if ((int)shape < 0 || (int)shape > 7) return fail(CS_ERR_INVALID_ARGUMENT, "unknown shape %d", (int)shape);
+    if (sem != CS_SEM_STEP && sem != CS_SEM_FUSED)
+        return fail(CS_ERR_INVALID_ARGUMENT, "unknown semantics %d", (int)sem);
+    if (prec != CS_PREC_FP64 && prec != CS_PREC_SPLIT)
+        return fail(CS_ERR_INVALID_ARGUMENT, "unknown precision %d", (int)prec);
+    if (!extent || !weights) return fail(CS_ERR_INVALID_ARGUMENT, "extent or weights is NULL");
+    const ShapeInfo &si = kShapes[shape];
+    const int need = sem == CS_SEM_STEP ? si.n_base : si.n_fused;
+    if (n_weights != need)
+        return fail(CS_ERR_INVALID_ARGUMENT, "%s (%s) takes %d weights, got %d", si.name,
+                    sem == CS_SEM_STEP ? "step" : "fused", need, n_weights);
+    for (int i = 0; i < need; ++i)
+        if (!std::isfinite(weights[i]))
+            return fail(CS_ERR_INVALID_ARGUMENT, "weight %d is not finite", i);
+    for (int d = 0; d < si.dims; ++d)
+        if (extent[d] < 1 || extent[d] > (1LL << 31) - 1)
+            return fail(CS_ERR_INVALID_ARGUMENT, "extent[%d] = %lld out of range", d, extent[d]);
+    cs_plan *p = new (std::nothrow) cs_plan();
+    if (!p) return fail(CS_ERR_OUT_OF_MEMORY, "plan allocation");
+    p->shape = shape;
+    p->sem = sem;
+    p->prec = prec;
+    p->dims = si.dims;
+    p->steps_per_sweep = sem == CS_SEM_STEP ? 1 : si.fused_steps;
+    expand_weights(shape, sem, weights, p->w, p->radius);
+    p->pattern = classify(p->w, p->dims, p->radius);
+    if (layout) {
+        const cs_layout &L = *layout;
+        bool ok = L.dims == si.dims && L.halo >= p->radius && L.pitch[si.dims - 1] == 1;
+        for (int d = 0; ok && d < si.dims; ++d) ok = L.extent[d] == extent[d] && L.pitch[d] >= 1;
+        if (ok && si.dims >= 2) ok = L.pitch[si.dims - 2] >= L.extent[si.dims - 1] + 2 * p->radius;
+        if (ok && si.dims == 3) ok = L.pitch[0] >= L.pitch[1] * (L.extent[1] + 2 * p->radius);
+        if (!ok) {
+            delete p;
+            return fail(CS_ERR_INVALID_ARGUMENT, "layout does not fit the grid with halo %d", p->radius);
+        }
+        p->layout = L;
+        p->layout.bytes = (size_t)L.elements * sizeof(double);
+    } else {
+        native_layout(si.dims, p->radius, extent, p->layout);
+    }
+    p->view.dims = si.dims;
+    for (int d = 0; d < 3; ++d) {
+        p->view.ext[d] = d < si.dims ? p->layout.extent[d] : 1;
+        p->view.pitch[d] = d < si.dims ? p->layout.pitch[d] : 1;
+    }
+    const bool supported = prec == CS_PREC_FP64
+                               ? cs::fp64_fma_supported(p->dims, p->radius, p->pattern)
+                               : cs::split_supported(p->dims, p->radius, p->pattern);
+    if (!supported) {
+        delete p;
+        return fail(CS_ERR_UNSUPPORTED, "no kernel for dims=%d radius=%d pattern=%d precision=%d",
+                    si.dims, p->radius, p->pattern, (int)prec);
+    }
+    *out = p;
+    return CS_OK;
+}
+
+CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
+{
+    if (!p) return fail(CS_ERR_INVALID_ARGUMENT, "plan is NULL");
+    switch (opt) {
+    case CS_OPT_ALGO:
+        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_MMA) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
+        if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
+            return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
+        if (v == CS_ALGO_SPLIT_MMA && p->prec != CS_PREC_SPLIT)
+            return fail(CS_ERR_INVALID_ARGUMENT, "split algo needs a split-precision plan");
+        if ((v == CS_ALGO_FP64_FMA || v == CS_ALGO_FP64_MMA) && p->prec != CS_PREC_FP64)
+            return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
+        p->algo = (int)v;
+        return CS_OK;
+    case CS_OPT_SPLIT_LEVELS:
+        if (v < 2 || v > 7) return fail(CS_ERR_INVALID_ARGUMENT, "split levels must be 2..7");
+        p->split_levels = (int)v;
+        return CS_OK;
+    case CS_OPT_REANCHOR_INTERVAL:
+        if (v < 0) return fail(CS_ERR_INVALID_ARGUMENT, "negative re-anchor interval");
+        p->reanchor = v;
+        return CS_OK;
+    case CS_OPT_TIME_BLOCK:
+        if (v < 0 || v > 16) return fail(CS_ERR_INVALID_ARGUMENT, "time block must be 0..16");
+        p->time_block = (int)v;
+        return CS_OK;
+    }
+    return fail(CS_ERR_INVALID_ARGUMENT, "unknown option %d", (int)opt);
+}
+
+CS_API cs_status cs_plan_get_layout(const cs_plan *p, cs_layout *out)
+{
+    if (!p || !out) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = p->layout;
+    return CS_OK;
+}
+
+CS_API cs_status cs_plan_sweeps(const cs_plan *p, long long steps, long long *sweeps)
+{
+    if (!p || !sweeps) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (steps < 0) return fail(CS_ERR_INVALID_ARGUMENT, "negative step count");
+    if (steps % p->steps_per_sweep)
+        return fail(CS_ERR_INVALID_ARGUMENT, "%lld steps is not a multiple of the %d steps of a fused sweep",
+                    steps, p->steps_per_sweep);
+    *sweeps = steps / p->steps_per_sweep;
+    return CS_OK;
+}
+
+CS_API cs_status cs_plan_destroy(cs_plan *p)
+{
+    delete p;
+    return CS_OK;
+}
+
+CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *stream, int *result_in_b)
+{
+    if (!p || !a || !b) return fail(CS_ERR_INVALID_ARGUMENT, "NULL plan or buffer");
+    if (a == b) return fail(CS_ERR_INVALID_ARGUMENT, "ping-pong buffers must differ");
+    long long sweeps = 0;
+    cs_status s = cs_plan_sweeps(p, steps, &sweeps);
+    if (s != CS_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    int algo = CS_ALGO_FP64_FMA;
+    if (sweeps > 0) {
+        s = choose_algo(p, a, b, st, &algo);
+        if (s != CS_OK) return s;
+    }
+    void *buf[2] = {a, b};
+    for (long long i = 0; i < sweeps; ++i) {
+        cudaError_t e = launch_sweep(p, algo, buf[i & 1], buf[(i + 1) & 1], st);
+        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && ((i + 1) % p->reanchor) == 0) {
+            e = cs::launch_split_reanchor(p->view, (float2 *)buf[(i + 1) & 1] + p->layout.origin, st);
+            if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
+        }
+    }
+    if (result_in_b) *result_in_b = (int)(sweeps & 1);
+    return CS_OK;
+}
+
+CS_API cs_status cs_split_from_fp64(const cs_plan *p, const double *src, void *dst, void *stream)
+{
+    if (!p || !src || !dst) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    cs_layout L = p->layout;
+    // Convert the whole buffer (interior and halo) so halos stay exact.
+    GridView flat{1, {L.elements, 1, 1}, {1, 1, 1}};
+    CS_CUDA(cs::launch_split_from_fp64(flat, 0, src, (float2 *)dst, (cudaStream_t)stream));
+    return CS_OK;
+}
+
+CS_API cs_status cs_split_to_fp64(const cs_plan *p, const void *src, double *dst, void *stream)
+{
+    if (!p || !src || !dst) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    cs_layout L = p->layout;
+    GridView flat{1, {L.elements, 1, 1}, {1, 1, 1}};
+    CS_CUDA(cs::launch_split_to_fp64(flat, 0, (const float2 *)src, dst, (cudaStream_t)stream));
+    return CS_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------
+// Host-buffer runs (the reference wrappers' contract).
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+// in_elems doubles from host_in into buffer 0 (buffer 1 zero), `sweeps`
+// sweeps, then out_elems doubles from result + out_offset to host_out.
+cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *host_out,
+                   size_t out_offset, size_t out_elems, long long steps, double *loop_seconds)
+{
+    long long sweeps = 0;
+    cs_status s = cs_plan_sweeps(p, steps, &sweeps);
+    if (s != CS_OK) return s;
+    const size_t bytes = p->layout.bytes;
+    const size_t elem_bytes = sizeof(double);
+    DevBuf d[2], stage;
+    CS_CUDA(cudaMalloc(&d[0].p, bytes));
+    CS_CUDA(cudaMalloc(&d[1].p, bytes));
+    CS_CUDA(cudaMemset(d[0].p, 0, bytes));
+    CS_CUDA(cudaMemset(d[1].p, 0, bytes));
+    if (p->prec == CS_PREC_FP64) {
+        CS_CUDA(cudaMemcpy(d[0].p, host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
+    } else {
+        CS_CUDA(cudaMalloc(&stage.p, bytes));
+        CS_CUDA(cudaMemset(stage.p, 0, bytes));
+        CS_CUDA(cudaMemcpy(stage.p, host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
+        s = cs_split_from_fp64(p, (const double *)stage.p, d[0].p, nullptr);
+        if (s != CS_OK) return s;
+    }
+    cudaEvent_t e0, e1;
+    CS_CUDA(cudaEventCreate(&e0));
+    CS_CUDA(cudaEventCreate(&e1));
+    CS_CUDA(cudaEventRecord(e0, nullptr));
+    int in_b = 0;
+    s = cs_run(p, d[0].p, d[1].p, steps, nullptr, &in_b);
+    if (s != CS_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return s;
+    }
+    CS_CUDA(cudaEventRecord(e1, nullptr));
+    CS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (loop_seconds) *loop_seconds = ms * 1e-3;
+    t_loop_seconds = ms * 1e-3;
+    const void *res = d[in_b].p;
+    if (p->prec == CS_PREC_SPLIT) {
+        s = cs_split_to_fp64(p, res, (double *)stage.p, nullptr);
+        if (s != CS_OK) return s;
+        res = stage.p;
+    }
+    CS_CUDA(cudaMemcpy(host_out, (const double *)res + out_offset, out_elems * elem_bytes,
+                       cudaMemcpyDeviceToHost));
+    return CS_OK;
+}
+
+cs_status make_ref_plan(cs_plan **p, cs_shape shape, const long long *ext, const double *params,
+                        const cs_layout &L)
+{
+    const ShapeInfo &si = kShapes[shape];
+    return cs_plan_create(p, shape, CS_SEM_FUSED, CS_PREC_FP64, ext, params, si.n_fused, &L);
+}
+
+void print_timing(const char *banner, bool secs_line, double secs, double points, int steps_mult,
+                  int times)
+{
+    if (!g_verbose.load()) return;
+    if (banner) printf("%s\n", banner);
+    printf("Time = %lld[ms]\n", (long long)(secs * 1e3));
+    if (secs_line) printf("%g\n", secs);
+    printf("GStencil/s = %f\n", points * (double)times * steps_mult / secs / 1e9);
+    fflush(stdout);
+}
+
+struct PlanGuard {
+    cs_plan *p = nullptr;
+    ~PlanGuard() { cs_plan_destroy(p); }
+};
+
+cs_status check_ref_args(const void *in, const void *out, const void *params, int times,
+                         std::initializer_list<int> dims)
+{
+    if (!in || !out || !params) return fail(CS_ERR_INVALID_ARGUMENT, "NULL buffer or params");
+    if (times < 0) return fail(CS_ERR_INVALID_ARGUMENT, "negative times");
+    for (int d : dims)
+        if (d < 1) return fail(CS_ERR_INVALID_ARGUMENT, "grid extent %d < 1", d);
+    return CS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+CS_API cs_status cs_run_host(cs_plan *p, const double *host_in, double *host_out, long long steps)
+{
+    if (!p || !host_in || !host_out) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    const size_t n = (size_t)p->layout.elements;
+    return host_run(p, host_in, n, host_out, 0, n, steps, nullptr);
+}
+
+// src/1d/gpu_1r.cu:227-302. Device grid n+7 (index 0 pad, halo 3); the
+// result is read back from device index 1 (src/1d/gpu_1r.cu:299).
+CS_API cs_status cs_gpu_1d1r(const double *in, double *out, const double *params, int times, int n)
+{
+    cs_status s = check_ref_args(in, out, params, times, {n});
+    if (s != CS_OK) return s;
+    cs_layout L{};
+    L.dims = 1;
+    L.halo = 3;
+    L.extent[0] = n;
+    L.pitch[0] = 1;
+    L.origin = 4;
+    L.elements = (long long)n + 7;
+    const long long ext[1] = {n};
+    PlanGuard g;
+    s = make_ref_plan(&g.p, CS_SHAPE_1D1R, ext, params, L);
+    if (s != CS_OK) return s;
+    double secs = 0;
+    s = host_run(g.p, in, (size_t)n + 7, out, 1, (size_t)n + 6, 3LL * times, &secs);
+    if (s == CS_OK) print_timing("ConvStencil(1D): ", false, secs, (double)n, 3, times);
+    return s;
+}
+
+// src/1d/gpu_2r.cu:85-159. Device grid n+8 (halo 4); n+7 values come back
+// (src/1d/gpu_2r.cu:156).
+CS_API cs_status cs_gpu_star_1d2r_step2(const double *in, double *out, const double *params,
+                                        int times, int n)
+{
+    cs_status s = check_ref_args(in, out, params, times, {n});
+    if (s != CS_OK) return s;
+    cs_layout L{};
+    L.dims = 1;
+    L.halo = 4;
+    L.extent[0] = n;
+    L.pitch[0] = 1;
+    L.origin = 4;
+    L.elements = (long long)n + 8;
+    const long long ext[1] = {n};
+    PlanGuard g;
+    s = make_ref_plan(&g.p, CS_SHAPE_1D2R, ext, params, L);
+    if (s != CS_OK) return s;
+    double secs = 0;
+    s = host_run(g.p, in, (size_t)n + 8, out, 0, (size_t)n + 7, 2LL * times, &secs);
+    if (s == CS_OK) print_timing(nullptr, false, secs, (double)n, 2, times);
+    return s;
+}
+
+static cs_status gpu_2d(cs_shape shape, const double *in, double *out, const double *params,
+                        int times, int m, int n, int steps_mult)
+{
+    cs_status s = check_ref_args(in, out, params, times, {m, n});
+    if (s != CS_OK) return s;
+    // (m+6) x (n+8), interior rows [3, m+3), cols [4, n+4) (src/2d/gpu.cu:359-360).
+    cs_layout L{};
+    L.dims = 2;
+    L.halo = 3;
+    L.extent[0] = m;
+    L.extent[1] = n;
+    L.pitch[0] = (long long)n + 8;
+    L.pitch[1] = 1;
+    L.origin = 3 * L.pitch[0] + 4;
+    L.elements = ((long long)m + 6) * L.pitch[0];
+    const long long ext[2] = {m, n};
+    PlanGuard g;
+    s = make_ref_plan(&g.p, shape, ext, params, L);
+    if (s != CS_OK) return s;
+    double secs = 0;
+    const size_t all = (size_t)L.elements;
+    s = host_run(g.p, in, all, out, 0, all, (long long)steps_mult * times, &secs);
+    if (s == CS_OK) print_timing("ConvStencil(2D): ", false, secs, (double)m * n, steps_mult, times);
+    return s;
+}
+
+// src/2d/gpu.cu:245-334 (3 steps per sweep).
+CS_API cs_status cs_gpu_box_2d1r(const double *in, double *out, const double *params, int times,
+                                 int m, int n)
+{
+    return gpu_2d(CS_SHAPE_BOX2D1R, in, out, params, times, m, n, 3);
+}
+
+// src/2d/gpu.cu:336-425 (1 step per sweep).
+CS_API cs_status cs_gpu_box_2d3r(const double *in, double *out, const double *params, int times,
+                                 int m, int n)
+{
+    return gpu_2d(CS_SHAPE_BOX2D3R, in, out, params, times, m, n, 1);
+}
+
+static cs_status gpu_3d(cs_shape shape, const double *in, double *out, const double *params,
+                        int times, int h, int m, int n, const char *banner)
+{
+    cs_status s = check_ref_args(in, out, params, times, {h, m, n});
+    if (s != CS_OK) return s;
+    // (h+6) x (m+6) x (n+6), halo 3 on every axis (src/3d/gpu_box.cu:475-478).
+    cs_layout L{};
+    L.dims = 3;
+    L.halo = 3;
+    L.extent[0] = h;
+    L.extent[1] = m;
+    L.extent[2] = n;
+    L.pitch[2] = 1;
+    L.pitch[1] = (long long)n + 6;
+    L.pitch[0] = L.pitch[1] * ((long long)m + 6);
+    L.origin = 3 * L.pitch[0] + 3 * L.pitch[1] + 3;
+    L.elements = ((long long)h + 6) * L.pitch[0];
+    const long long ext[3] = {h, m, n};
+    PlanGuard g;
+    s = make_ref_plan(&g.p, shape, ext, params, L);
+    if (s != CS_OK) return s;
+    double secs = 0;
+    const size_t all = (size_t)L.elements;
+    s = host_run(g.p, in, all, out, 0, all, 3LL * times, &secs);
+    if (s == CS_OK) print_timing(banner, true, secs, (double)h * m * n, 3, times);
+    return s;
+}
+
+// src/3d/gpu_box.cu:446-536.
+CS_API cs_status cs_gpu_box_3d1r(const double *in, double *out, const double *params, int times,
+                                 int h, int m, int n)
+{
+    return gpu_3d(CS_SHAPE_BOX3D1R, in, out, params, times, h, m, n, "ConvStencil(3D): ");
+}
+
+// src/3d/gpu_star.cu:238-332.
+CS_API cs_status cs_gpu_star_3d1r(const double *in, double *out, const double *params, int times,
+                                  int h, int m, int n)
+{
+    return gpu_3d(CS_SHAPE_STAR3D1R, in, out, params, times, h, m, n, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+// cs_internal.h — shared declarations between the host library and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace cs {
+
+// Tap patterns a kernel can be specialised for. A dense (2r+1)^d weight array
+// is classified on the host into the smallest pattern that covers its
+// non-zero taps, so zero taps cost no FP64 instructions.
+enum Pattern : int {
+    PAT_DENSE = 0,   // every tap of the (2r+1)^d box
+    PAT_STAR = 1,    // axis-aligned cross: taps with at most one non-zero offset
+    PAT_DIAMOND = 2  // L1 ball: |d0| + |d1| (+ |d2|) <= r  (2D diamond, 3D octahedron)
+};
+
+constexpr int kMaxTaps = 343;  // 7^3
+
+struct Weights {
+    double v[kMaxTaps];
+};
+
+// A grid as the kernels see it: pointer to interior point (0,..,0), extents and
+// pitches slowest axis first (pitch of the last axis is 1).
+struct GridView {
+    int dims;
+    long long ext[3];
+    long long pitch[3];
+};
+
+// Kernel entry points (cs_kernels_fp64.cu). Each launches one sweep
+// in -> out on `stream`; `in`/`out` address interior point 0. Returns
+// cudaSuccess or the launch error.
+cudaError_t launch_fp64_fma(const GridView &g, int radius, int pattern, const Weights &w,
+                            const double *in, double *out, cudaStream_t stream);
+// FP64 tensor-core path (mma.sync m8n8k4.f64), 2D radius-3 dense kernels only.
+cudaError_t launch_fp64_mma_2d(const GridView &g, const Weights &w, const double *in, double *out,
+                               cudaStream_t stream);
+bool fp64_fma_supported(int dims, int radius, int pattern);
+
+// Split precision (cs_kernels_split.cu). Grids hold float2 (hi, lo) pairs.
+struct SplitWeights;  // defined in cs_kernels_split.cu
+cudaError_t launch_split_sweep(const GridView &g, int radius, int pattern, const Weights &w,
+                               int levels, const float2 *in, float2 *out, cudaStream_t stream);
+bool split_supported(int dims, int radius, int pattern);
+cudaError_t launch_split_from_fp64(const GridView &g, int halo, const double *src, float2 *dst,
+                                   cudaStream_t stream);
+cudaError_t launch_split_to_fp64(const GridView &g, int halo, const float2 *src, double *dst,
+                                 cudaStream_t stream);
+cudaError_t launch_split_reanchor(const GridView &g, float2 *grid, cudaStream_t stream);
+
+// Process-wide launch counter (host side), for the bench's launch accounting.
+void note_launch(long long n = 1);
+
+}  // namespace cs

@@ -1,0 +1,180 @@
+/*
+ * convstencil.h — C ABI of the GB300-native ConvStencil library
+ * (libconvstencil_gb300.so).
+ *
+ * Two surfaces:
+ *
+ * 1. Reference-shaped wrappers, one per host wrapper of microsoft/ConvStencil.
+ *    Same arguments, layouts and meaning; a status code instead of exit()/abort().
+ *    Host buffers in and out, device memory allocated and released inside the
+ *    call (the reference leaks it), timing lines printed to stdout only when
+ *    `cs_set_verbose(1)` (the C++-linkage drop-in symbols in
+ *    convstencil_ref.h always print, as the reference does).
+ *
+ * 2. Plans over caller-owned DEVICE buffers: reentrant (no global state, no
+ *    __constant__ symbols; weights travel in kernel parameters), explicit
+ *    CUDA stream, any layout with a zero halo, FP64 or split precision.
+ *
+ * All functions return CS_OK or an error code; cs_last_error() gives a
+ * per-thread message for the last failure. Nothing here exits or aborts.
+ */
+#ifndef CONVSTENCIL_H
+#define CONVSTENCIL_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CS_API __attribute__((visibility("default")))
+
+typedef enum cs_status {
+    CS_OK = 0,
+    CS_ERR_INVALID_ARGUMENT = 1, /* bad shape, size, pointer, weight count */
+    CS_ERR_UNSUPPORTED = 2,      /* valid request this build does not serve */
+    CS_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    CS_ERR_OUT_OF_MEMORY = 4,    /* device or host allocation failed */
+    CS_ERR_TIMEOUT = 5,          /* a bounded device-side wait expired */
+    CS_ERR_NO_DEVICE = 6         /* no usable CUDA device */
+} cs_status;
+
+/* The eight stencil shapes of the reference CLIs (src/1d/main.cu:69-79,
+ * src/2d/main.cu:138-160, src/3d/main.cu:489-500). */
+typedef enum cs_shape {
+    CS_SHAPE_1D1R = 0,     /* 3-point, radius 1 */
+    CS_SHAPE_1D2R = 1,     /* 5-point, radius 2 */
+    CS_SHAPE_STAR2D1R = 2, /* 5-point cross, radius 1 */
+    CS_SHAPE_BOX2D1R = 3,  /* 3x3 box */
+    CS_SHAPE_STAR2D3R = 4, /* 13-point cross, radius 3 */
+    CS_SHAPE_BOX2D3R = 5,  /* 7x7 box */
+    CS_SHAPE_STAR3D1R = 6, /* 7-point cross, radius 1 */
+    CS_SHAPE_BOX3D1R = 7   /* 3x3x3 box */
+} cs_shape;
+
+/* What one "sweep" means.
+ * CS_SEM_STEP : weights are the base stencil's (3, 5, 5, 9, 13, 49, 7, 27
+ *               values, row-major over the cells of the shape); a step is
+ *               one sweep of that stencil with a zero halo of its radius.
+ * CS_SEM_FUSED: weights are the reference wrappers' fused parameters
+ *               (7, 9, 49, 49, 49, 49, 44, 196 values); a sweep applies the
+ *               fused kernel once with a zero halo of the fused radius, and
+ *               counts as 3 steps (1d1r, 2d1r shapes, 3D shapes), 2 (1d2r)
+ *               or 1 (2d3r shapes), as the reference counts it
+ *               (src/2d/gpu.cu:329, src/1d/gpu_2r.cu:154, src/3d/gpu_box.cu:531). */
+typedef enum cs_semantics { CS_SEM_STEP = 0, CS_SEM_FUSED = 1 } cs_semantics;
+
+/* Arithmetic of the sweep.
+ * CS_PREC_FP64 : FP64 grids, FP64 arithmetic (FP64 FMA or FP64 MMA).
+ * CS_PREC_SPLIT: grids stored as FP32 (hi, lo) pairs (8 bytes per point);
+ *                the contraction runs on BF16 tensor cores over exact
+ *                fixed-point slices with FP32 accumulation; see
+ *                CS_OPT_SPLIT_LEVELS for the accuracy/speed trade. */
+typedef enum cs_precision { CS_PREC_FP64 = 0, CS_PREC_SPLIT = 1 } cs_precision;
+
+/* Kernel family; CS_ALGO_AUTO lets the plan's tuner choose. */
+typedef enum cs_algo {
+    CS_ALGO_AUTO = 0,
+    CS_ALGO_FP64_FMA = 1, /* FP64 FMA, one output per tap-FMA (fewest FP64 ops) */
+    CS_ALGO_FP64_MMA = 2, /* FP64 tensor-core MMA (mma.sync m8n8k4.f64), 2x4 output blocks */
+    CS_ALGO_SPLIT_MMA = 3 /* split precision on BF16 tensor cores */
+} cs_algo;
+
+typedef enum cs_option {
+    CS_OPT_ALGO = 0,             /* cs_algo */
+    CS_OPT_SPLIT_LEVELS = 1,     /* 2..7 slice levels (default 5: <= 1e-10 rel.) */
+    CS_OPT_REANCHOR_INTERVAL = 2,/* split: renormalise (hi,lo) in FP64 every N steps (default 100, 0 = never) */
+    CS_OPT_TIME_BLOCK = 3        /* steps fused per launch by temporal blocking (0 = tuner) */
+} cs_option;
+
+/* Where a grid lives in a buffer. extent/pitch are slowest axis first; the
+ * last axis is contiguous (pitch 1). `origin` is the element offset of
+ * interior point (0,...,0). Every interior point must have `halo` cells of
+ * zeros (or of the caller's fixed boundary values) around it in memory. */
+typedef struct cs_layout {
+    int dims;
+    int halo;
+    long long extent[3];
+    long long pitch[3];
+    long long origin;
+    long long elements; /* elements per buffer */
+    size_t bytes;       /* bytes per buffer */
+} cs_layout;
+
+typedef struct cs_plan cs_plan;
+
+/* ---- plans over device buffers --------------------------------------- */
+
+/* extent: `dims` interior sizes, slowest first. weights: see cs_semantics.
+ * layout: NULL for the library's native layout (rows padded to 16 bytes,
+ * halo = the sweep's radius), or the caller's own layout. */
+CS_API cs_status cs_plan_create(cs_plan **plan, cs_shape shape, cs_semantics sem,
+                                cs_precision prec, const long long *extent,
+                                const double *weights, int n_weights,
+                                const cs_layout *layout);
+CS_API cs_status cs_plan_set_option(cs_plan *plan, cs_option opt, long long value);
+CS_API cs_status cs_plan_get_layout(const cs_plan *plan, cs_layout *out);
+/* Sweep count and steps per sweep for `steps` steps (FUSED: steps must be a
+ * multiple of the fused step count). */
+CS_API cs_status cs_plan_sweeps(const cs_plan *plan, long long steps, long long *sweeps);
+CS_API cs_status cs_plan_destroy(cs_plan *plan);
+
+/* Runs `steps` steps from buffer a, ping-ponging with b (both per the plan's
+ * layout, halos zero, both device pointers). *result_in_b is set to 1 when
+ * the final grid is in b. Asynchronous on `stream` (a cudaStream_t; NULL =
+ * legacy default stream). */
+CS_API cs_status cs_run(cs_plan *plan, void *a, void *b, long long steps, void *stream,
+                        int *result_in_b);
+
+/* Split precision: FP64 grid <-> (hi, lo) FP32 pairs, same layout. */
+CS_API cs_status cs_split_from_fp64(const cs_plan *plan, const double *src, void *dst, void *stream);
+CS_API cs_status cs_split_to_fp64(const cs_plan *plan, const void *src, double *dst, void *stream);
+
+/* Host-buffer form of cs_run: allocates two device grids, copies host_in
+ * (FP64, plan layout) in, runs, copies the result (FP64) to host_out,
+ * releases everything. Synchronous. */
+CS_API cs_status cs_run_host(cs_plan *plan, const double *host_in, double *host_out,
+                             long long steps);
+
+/* ---- reference-shaped wrappers (FUSED semantics, reference layouts) ---- */
+/* Replaces gpu_1d1r (src/1d/1d_utils.h:75, src/1d/gpu_1r.cu:227-302).
+ * in: n+7 doubles (index 0 alignment pad, halo 3); out: n+6 doubles, the
+ * device array from index 1 (src/1d/gpu_1r.cu:299). params: 7. */
+CS_API cs_status cs_gpu_1d1r(const double *in, double *out, const double *params,
+                             int times, int input_n);
+/* Replaces gpu_star_1d2r_step2 (src/1d/1d_utils.h:85, src/1d/gpu_2r.cu:85-159).
+ * in: n+8 doubles (halo 4); out: n+7 doubles (src/1d/gpu_2r.cu:156). params: 9. */
+CS_API cs_status cs_gpu_star_1d2r_step2(const double *in, double *out, const double *params,
+                                        int times, int input_n);
+/* Replaces gpu_box_2d1r (src/2d/2d_utils.h:77, src/2d/gpu.cu:245-334).
+ * in/out: (m+6) x (n+8) doubles; params: 49; counts 3 steps per sweep. */
+CS_API cs_status cs_gpu_box_2d1r(const double *in, double *out, const double *params,
+                                 int times, int input_m, int input_n);
+/* Replaces gpu_box_2d3r (src/2d/2d_utils.h:79, src/2d/gpu.cu:336-425). */
+CS_API cs_status cs_gpu_box_2d3r(const double *in, double *out, const double *params,
+                                 int times, int input_m, int input_n);
+/* Replaces gpu_box_3d1r (src/3d/3d_utils.h:75, src/3d/gpu_box.cu:446-536).
+ * in/out: (h+6) x (m+6) x (n+6); params: 196 (4 planes, plane p <-> |dz|=3-p). */
+CS_API cs_status cs_gpu_box_3d1r(const double *in, double *out, const double *params,
+                                 int times, int input_h, int input_m, int input_n);
+/* Replaces gpu_star_3d1r (src/3d/3d_utils.h:85, src/3d/gpu_star.cu:238-332).
+ * params: 44 (octahedron cells by plane, src/3d/gpu_star.cu:30-56). */
+CS_API cs_status cs_gpu_star_3d1r(const double *in, double *out, const double *params,
+                                  int times, int input_h, int input_m, int input_n);
+
+/* ---- utilities --------------------------------------------------------- */
+CS_API const char *cs_status_string(cs_status s);
+CS_API const char *cs_last_error(void);
+CS_API void cs_set_verbose(int on);
+/* Seconds of GPU time of the last timed loop run by a reference-shaped
+ * wrapper on this thread (CUDA events around the launch loop). */
+CS_API double cs_last_loop_seconds(void);
+/* Number of kernel launches issued by this process so far. */
+CS_API long long cs_kernel_launch_count(void);
+/* Library version string. */
+CS_API const char *cs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CONVSTENCIL_H */
