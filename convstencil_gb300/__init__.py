@@ -75,13 +75,12 @@ class Algo(enum.IntEnum):
     FP64_FMA = 1
     FP64_MMA = 2
     SPLIT_MMA = 3
+    SPLIT_FMA = 4
 
 
 class Option(enum.IntEnum):
     ALGO = 0
-    SPLIT_LEVELS = 1
     REANCHOR_INTERVAL = 2
-    TIME_BLOCK = 3
 
 
 class Layout(ctypes.Structure):

@@ -217,9 +217,7 @@ struct cs_plan {
     cs_layout layout;
     GridView view;
     int algo = CS_ALGO_AUTO;
-    int split_levels = 5;
     long long reanchor = 100;
-    int time_block = 0;
 };
 
 namespace {
@@ -228,6 +226,16 @@ bool fp64_mma_ok(const cs_plan *p)
 {
     return p->prec == CS_PREC_FP64 && p->dims == 2 && p->radius == 3 &&
            p->pattern == cs::PAT_DENSE;
+}
+
+// The slice kernel's error is relative to the tile scale times the largest
+// weight; on grids smaller than the 8x8 window every output can be formed by
+// a few small taps only, so those go to the double-float kernel.
+bool split_mma_ok(const cs_plan *p)
+{
+    return p->prec == CS_PREC_SPLIT && p->dims == 2 && p->radius == 3 &&
+           p->view.ext[0] >= 8 && p->view.ext[1] >= 8 &&
+           cs::split_mma_layout_ok(p->view, p->layout.origin);
 }
 
 cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *out_base,
@@ -242,8 +250,8 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
     }
     const float2 *in = (const float2 *)in_base + off;
     float2 *out = (float2 *)out_base + off;
-    return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, p->split_levels, in, out,
-                                  st);
+    return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, algo == CS_ALGO_SPLIT_MMA,
+                                  in, out, st);
 }
 
 int size_class(const cs_plan *p)
@@ -264,17 +272,29 @@ int size_class(const cs_plan *p)
 // no result) and the winner is remembered for plans of the same class.
 cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *out)
 {
+    int cand[2];
     if (p->prec == CS_PREC_SPLIT) {
-        *out = CS_ALGO_SPLIT_MMA;
-        return CS_OK;
-    }
-    if (p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) {
-        *out = CS_ALGO_FP64_MMA;
-        return CS_OK;
-    }
-    if (p->algo != CS_ALGO_AUTO || !fp64_mma_ok(p)) {
-        *out = CS_ALGO_FP64_FMA;
-        return CS_OK;
+        if (p->algo == CS_ALGO_SPLIT_FMA || !split_mma_ok(p)) {
+            *out = CS_ALGO_SPLIT_FMA;
+            return CS_OK;
+        }
+        if (p->algo == CS_ALGO_SPLIT_MMA) {
+            *out = CS_ALGO_SPLIT_MMA;
+            return CS_OK;
+        }
+        cand[0] = CS_ALGO_SPLIT_MMA;
+        cand[1] = CS_ALGO_SPLIT_FMA;
+    } else {
+        if (p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) {
+            *out = CS_ALGO_FP64_MMA;
+            return CS_OK;
+        }
+        if (p->algo != CS_ALGO_AUTO || !fp64_mma_ok(p)) {
+            *out = CS_ALGO_FP64_FMA;
+            return CS_OK;
+        }
+        cand[0] = CS_ALGO_FP64_FMA;
+        cand[1] = CS_ALGO_FP64_MMA;
     }
     auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
     {
@@ -285,9 +305,8 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
             return CS_OK;
         }
     }
-    const int cand[2] = {CS_ALGO_FP64_FMA, CS_ALGO_FP64_MMA};
     float best_ms = 1e30f;
-    int best = CS_ALGO_FP64_FMA;
+    int best = cand[0];
     cudaEvent_t e0, e1;
     CS_CUDA(cudaEventCreate(&e0));
     CS_CUDA(cudaEventCreate(&e1));
@@ -408,26 +427,21 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
     if (!p) return fail(CS_ERR_INVALID_ARGUMENT, "plan is NULL");
     switch (opt) {
     case CS_OPT_ALGO:
-        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_MMA) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
-        if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
-            return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
-        if (v == CS_ALGO_SPLIT_MMA && p->prec != CS_PREC_SPLIT)
+        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_FMA) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
+        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_FMA) && p->prec != CS_PREC_SPLIT)
             return fail(CS_ERR_INVALID_ARGUMENT, "split algo needs a split-precision plan");
         if ((v == CS_ALGO_FP64_FMA || v == CS_ALGO_FP64_MMA) && p->prec != CS_PREC_FP64)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
+        if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
+            return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
+        if (v == CS_ALGO_SPLIT_MMA && !split_mma_ok(p))
+            return fail(CS_ERR_UNSUPPORTED,
+                        "split MMA serves 2D radius-3 plans of at least 8x8 on even-aligned layouts");
         p->algo = (int)v;
-        return CS_OK;
-    case CS_OPT_SPLIT_LEVELS:
-        if (v < 2 || v > 7) return fail(CS_ERR_INVALID_ARGUMENT, "split levels must be 2..7");
-        p->split_levels = (int)v;
         return CS_OK;
     case CS_OPT_REANCHOR_INTERVAL:
         if (v < 0) return fail(CS_ERR_INVALID_ARGUMENT, "negative re-anchor interval");
         p->reanchor = v;
-        return CS_OK;
-    case CS_OPT_TIME_BLOCK:
-        if (v < 0 || v > 16) return fail(CS_ERR_INVALID_ARGUMENT, "time block must be 0..16");
-        p->time_block = (int)v;
         return CS_OK;
     }
     return fail(CS_ERR_INVALID_ARGUMENT, "unknown option %d", (int)opt);
@@ -475,7 +489,7 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
         cudaError_t e = launch_sweep(p, algo, buf[i & 1], buf[(i + 1) & 1], st);
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && ((i + 1) % p->reanchor) == 0) {
-            e = cs::launch_split_reanchor(p->view, (float2 *)buf[(i + 1) & 1] + p->layout.origin, st);
+            e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[(i + 1) & 1], st);
             if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
         }
     }
@@ -486,19 +500,15 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
 CS_API cs_status cs_split_from_fp64(const cs_plan *p, const double *src, void *dst, void *stream)
 {
     if (!p || !src || !dst) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
-    cs_layout L = p->layout;
-    // Convert the whole buffer (interior and halo) so halos stay exact.
-    GridView flat{1, {L.elements, 1, 1}, {1, 1, 1}};
-    CS_CUDA(cs::launch_split_from_fp64(flat, 0, src, (float2 *)dst, (cudaStream_t)stream));
+    // Converts the whole buffer (interior and halo) so halos stay exact.
+    CS_CUDA(cs::launch_split_from_fp64(p->layout.elements, src, (float2 *)dst, (cudaStream_t)stream));
     return CS_OK;
 }
 
 CS_API cs_status cs_split_to_fp64(const cs_plan *p, const void *src, double *dst, void *stream)
 {
     if (!p || !src || !dst) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
-    cs_layout L = p->layout;
-    GridView flat{1, {L.elements, 1, 1}, {1, 1, 1}};
-    CS_CUDA(cs::launch_split_to_fp64(flat, 0, (const float2 *)src, dst, (cudaStream_t)stream));
+    CS_CUDA(cs::launch_split_to_fp64(p->layout.elements, (const float2 *)src, dst, (cudaStream_t)stream));
     return CS_OK;
 }
 

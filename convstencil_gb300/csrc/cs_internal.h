@@ -42,15 +42,16 @@ cudaError_t launch_fp64_mma_2d(const GridView &g, const Weights &w, const double
 bool fp64_fma_supported(int dims, int radius, int pattern);
 
 // Split precision (cs_kernels_split.cu). Grids hold float2 (hi, lo) pairs.
-struct SplitWeights;  // defined in cs_kernels_split.cu
+// use_mma selects the FP16 tensor-core slice kernel (2D, radius 3, layouts
+// accepted by split_mma_layout_ok), otherwise double-float FP32 kernels run.
 cudaError_t launch_split_sweep(const GridView &g, int radius, int pattern, const Weights &w,
-                               int levels, const float2 *in, float2 *out, cudaStream_t stream);
+                               int use_mma, const float2 *in, float2 *out, cudaStream_t stream);
 bool split_supported(int dims, int radius, int pattern);
-cudaError_t launch_split_from_fp64(const GridView &g, int halo, const double *src, float2 *dst,
-                                   cudaStream_t stream);
-cudaError_t launch_split_to_fp64(const GridView &g, int halo, const float2 *src, double *dst,
-                                 cudaStream_t stream);
-cudaError_t launch_split_reanchor(const GridView &g, float2 *grid, cudaStream_t stream);
+bool split_mma_layout_ok(const GridView &g, long long origin);
+// Whole-buffer conversions and re-anchoring over n elements.
+cudaError_t launch_split_from_fp64(long long n, const double *src, float2 *dst, cudaStream_t stream);
+cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cudaStream_t stream);
+cudaError_t launch_split_reanchor(long long n, float2 *grid, cudaStream_t stream);
 
 // Process-wide launch counter (host side), for the bench's launch accounting.
 void note_launch(long long n = 1);

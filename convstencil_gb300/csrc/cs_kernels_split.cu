@@ -1,9 +1,430 @@
-// cs_kernels_split.cu — split-precision grids: FP32 (hi, lo) pairs.
+// cs_kernels_split.cu — split-precision sweeps: grids of FP32 (hi, lo) pairs.
+//
+// A value is x = hi + lo with |lo| <= ulp(hi)/2 (about 48 significant bits,
+// 8 bytes per point, the same HBM traffic as FP64). GB300 runs FP32 at ~63x
+// and FP16 tensor MMA at ~550x the FP64 rate, so the sweeps avoid FP64 math:
+//
+//  * k*_ff: double-float arithmetic on FP32 cores. Per tap: an exact product
+//    of the high parts (TwoProd via FMA), an error-free TwoSum into the
+//    running sum, and the cross terms hi*lo in plain FP32. About 12 FP32 ops
+//    per tap; error ~2^-44 per sweep. Used for the small stencils (3 to 27
+//    taps), which stay HBM-bound with it.
+//
+//  * k2d_mma: exact fixed-point slices on FP16 tensor cores, for dense 7x7
+//    kernels (box2d3r and the reference's fused 2D kernels). Per CTA tile the
+//    inputs are scaled by a power of two 2^-E so |x'| < 1/2 and cut into five
+//    balanced 9-bit digits d_k (|d_k| <= 256, exact in FP16); the weights are
+//    cut the same way (e_l, scale = the largest weight). A product d_k*e_l is
+//    an integer of at most 16 bits, and one level s = k + l holds at most 5
+//    pairs, so a level's 49-tap sum stays below 5*49*2^16 < 2^24: the FP32
+//    accumulators of mma.sync.m16n8k16 hold every level EXACTLY. Levels 0..4
+//    (15 pairs) are kept: 45 bits of each operand, dropped terms below ~2^-47
+//    of the scale, and a weight 2^-8 below the largest still carries ~37
+//    bits. The five level sums are recombined with error-free transformations
+//    into a (hi, lo) pair. Outputs are 2x4 blocks: one MMA column per output
+//    of a block, one MMA row per block, K = the 8x10 input window of a block
+//    (80 = 5 k-steps of 16).
 #include "cs_internal.h"
 
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
 namespace cs {
+
+struct SplitWeights {
+    float hi[kMaxTaps];
+    float lo[kMaxTaps];
+};
+
 namespace {
 
+// ------------------------------------------------------- error-free pieces
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// One tap of a double-float dot product: (sh, sl) += (wh + wl) * (xh + xl).
+__device__ __forceinline__ void ff_tap(float &sh, float &sl, float wh, float wl, float xh, float xl)
+{
+    const float p = wh * xh;
+    const float ep = fmaf(wh, xh, -p);  // exact error of the product
+    float s, q;
+    two_sum(sh, p, s, q);
+    sh = s;
+    sl += q;
+    sl += ep;
+    sl = fmaf(wh, xl, sl);
+    sl = fmaf(wl, xh, sl);
+}
+
+__device__ __forceinline__ float2 ff_finish(float sh, float sl)
+{
+    float h, l;
+    two_sum(sh, sl, h, l);
+    return make_float2(h, l);
+}
+
+template <int K>
+struct FW {
+    float hi[K];
+    float lo[K];
+};
+
+__host__ __device__ constexpr int iabs_(int x) { return x < 0 ? -x : x; }
+
+template <int P, int R>
+__host__ __device__ constexpr bool tap2s(int i, int j)
+{
+    return P == PAT_DENSE ? true : P == PAT_STAR ? (i == R || j == R) : (iabs_(i - R) + iabs_(j - R) <= R);
+}
+
+template <int P, int R>
+__host__ __device__ constexpr bool tap3s(int a, int i, int j)
+{
+    return P == PAT_DENSE ? true
+           : P == PAT_STAR ? ((a != R) + (i != R) + (j != R) <= 1)
+                           : (iabs_(a - R) + iabs_(i - R) + iabs_(j - R) <= R);
+}
+
+// ----------------------------------------------------------- CUDA-core forms
+template <int R>
+__global__ void __launch_bounds__(256) k1d_ff(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                              long long n, FW<2 * R + 1> w)
+{
+    constexpr int T = 1024;
+    __shared__ float2 s[T + 2 * R];
+    const long long x0 = (long long)blockIdx.x * T;
+    for (int i = threadIdx.x; i < T + 2 * R; i += blockDim.x) {
+        const long long gx = x0 - R + i;
+        s[i] = (gx < n + R) ? in[gx] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < T / 256; ++p) {
+        const int lx = threadIdx.x + p * 256;
+        float sh = 0.f, sl = 0.f;
+#pragma unroll
+        for (int t = 0; t <= 2 * R; ++t) ff_tap(sh, sl, w.hi[t], w.lo[t], s[lx + t].x, s[lx + t].y);
+        const long long gx = x0 + lx;
+        if (gx < n) out[gx] = ff_finish(sh, sl);
+    }
+}
+
+template <int R, int P>
+__global__ void __launch_bounds__(256) k2d_ff(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                              int m, int n, long long ld,
+                                              FW<(2 * R + 1) * (2 * R + 1)> w)
+{
+    constexpr int K = 2 * R + 1, TX = 64, TY = 32, RPT = 8;
+    constexpr int SX = TX + 2 * R, SY = TY + 2 * R;
+    __shared__ float2 s[SY * SX];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    for (int idx = threadIdx.x; idx < SY * SX; idx += blockDim.x) {
+        const int sy = idx / SX, sx = idx - sy * SX;
+        const int gy = y0 - R + sy, gx = x0 - R + sx;
+        s[idx] = (gy < m + R && gx < n + R) ? in[(long long)gy * ld + gx] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
+    float sh[RPT], sl[RPT];
+#pragma unroll
+    for (int o = 0; o < RPT; ++o) sh[o] = sl[o] = 0.f;
+    const float2 *col = s + (g * RPT) * SX + c;
+#pragma unroll
+    for (int ir = 0; ir < RPT + 2 * R; ++ir) {
+        float2 v[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) v[j] = col[ir * SX + j];
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            const int o = ir - i;
+            if (o >= 0 && o < RPT) {
+#pragma unroll
+                for (int j = 0; j < K; ++j)
+                    if (tap2s<P, R>(i, j))
+                        ff_tap(sh[o], sl[o], w.hi[i * K + j], w.lo[i * K + j], v[j].x, v[j].y);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < RPT; ++o) {
+        const int y = y0 + g * RPT + o, x = x0 + c;
+        if (y < m && x < n) out[(long long)y * ld + x] = ff_finish(sh[o], sl[o]);
+    }
+}
+
+template <int R, int P>
+__global__ void __launch_bounds__(256) k3d_ff(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                              int h, int m, int n, long long ldy, long long ldz, int zc,
+                                              FW<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
+{
+    constexpr int K = 2 * R + 1, TX = 32, TY = 16;
+    constexpr int SX = TX + 2 * R, SY = TY + 2 * R, PL = SX * SY;
+    extern __shared__ float2 ring2[];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+    const int zend = min(z0 + zc, h);
+    auto load_plane = [&](int gz) {
+        float2 *dst = ring2 + ((gz + K) % K) * PL;
+        const bool zok = gz < h + R;
+        for (int idx = threadIdx.x; idx < PL; idx += blockDim.x) {
+            const int sy = idx / SX, sx = idx - sy * SX;
+            const int gy = y0 - R + sy, gx = x0 - R + sx;
+            dst[idx] = (zok && gy < m + R && gx < n + R)
+                           ? in[(long long)gz * ldz + (long long)gy * ldy + gx]
+                           : make_float2(0.f, 0.f);
+        }
+    };
+    for (int gz = z0 - R; gz < z0 + R; ++gz) load_plane(gz);
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    for (int z = z0; z < zend; ++z) {
+        load_plane(z + R);
+        __syncthreads();
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+            const int ly = ly0 + 8 * q;
+            float sh = 0.f, sl = 0.f;
+#pragma unroll
+            for (int a = 0; a < K; ++a) {
+                const float2 *pl = ring2 + ((z - R + a + K) % K) * PL + ly * SX + lx;
+#pragma unroll
+                for (int i = 0; i < K; ++i)
+#pragma unroll
+                    for (int j = 0; j < K; ++j)
+                        if (tap3s<P, R>(a, i, j)) {
+                            const float2 v = pl[i * SX + j];
+                            const int t = (a * K + i) * K + j;
+                            ff_tap(sh, sl, w.hi[t], w.lo[t], v.x, v.y);
+                        }
+            }
+            const int y = y0 + ly, x = x0 + lx;
+            if (y < m && x < n) out[(long long)z * ldz + (long long)y * ldy + x] = ff_finish(sh, sl);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------- tensor-core form
+constexpr int kDigits = 5;       // x and w slices
+constexpr int kDigitBits = 9;    // balanced base-512 digits, |d| <= 256
+constexpr float kRadix = 512.f;
+
+struct SliceWeights {
+    __half d[kDigits][49];  // digits of w / 2^Ew, row-major 7x7
+    int ew;                 // weight scale exponent: |w| < 2^(ew-1)
+};
+
+__device__ __forceinline__ void mma16816(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ unsigned pack_h2(float lo_elem, float hi_elem)
+{
+    const __half2 h = __floats2half2_rn(lo_elem, hi_elem);  // .x = first (lower address)
+    return *reinterpret_cast<const unsigned *>(&h);
+}
+
+// Cuts x' = (a + b) (|x'| < 256 after the first scaling) into five balanced
+// base-512 digits. Every step is exact: rint(a) is an integer within 1/2 of
+// a, a - rint(a) is representable, and two_sum keeps (a, b) normalised.
+__device__ __forceinline__ void slice_digits(float a, float b, float (&d)[kDigits])
+{
+#pragma unroll
+    for (int k = 0; k < kDigits - 1; ++k) {
+        d[k] = rintf(a);
+        float s, e;
+        two_sum(a - d[k], b, s, e);
+        a = s * kRadix;
+        b = e * kRadix;
+    }
+    d[kDigits - 1] = rintf(a + b);
+}
+
+constexpr int MT_X = 64, MT_Y = 32;              // CTA output tile
+constexpr int SL_X = MT_X + 6, SL_Y = MT_Y + 6;  // input tile with radius-3 halo
+// Halves per slice row. 102 halves = 51 words = 19 mod 32 banks: when the
+// K indices of one A-fragment load straddle two window rows, the two rows'
+// words land in disjoint banks.
+constexpr int SL_PITCH = 102;
+constexpr int SL_PLANE = SL_Y * SL_PITCH;
+
+// Persistent: each CTA walks tiles tile = blockIdx.x, +gridDim.x, ...; the
+// weight digits are staged in shared memory and turned into B fragments once.
+__global__ void __launch_bounds__(256, 2) k2d_mma(const float2 *__restrict__ in,
+                                                  float2 *__restrict__ out, int m, int n,
+                                                  long long ld, int tiles_x, int tiles,
+                                                  SliceWeights sw)
+{
+    __shared__ __align__(16) __half sl[kDigits][SL_PLANE];
+    __shared__ __half wd[kDigits * 49];
+    __shared__ float red[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+
+    for (int i = tid; i < kDigits * 49; i += blockDim.x) wd[i] = sw.d[i / 49][i % 49];
+    __syncthreads();
+    // B fragments (weights' digits) for this lane: column n = g of the 2x4
+    // block (a = g/4, b = g%4), rows kk = 16s + {2t, 2t+1, 2t+8, 2t+9};
+    // B[kk][n] = w[r-a][j-b] with kk = 10r + j.
+    unsigned bf[kDigits][5][2];
+    {
+        const int a = g >> 2, b = g & 3;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                float e[kDigits][2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int kk = 16 * s + 2 * t + 8 * half + u;
+                    const int r = kk / 10, j = kk - 10 * r;
+                    const int ri = r - a, ci = j - b;
+                    const bool in_w = ri >= 0 && ri < 7 && ci >= 0 && ci < 7;
+#pragma unroll
+                    for (int l = 0; l < kDigits; ++l)
+                        e[l][u] = in_w ? __half2float(wd[l * 49 + ri * 7 + ci]) : 0.f;
+                }
+#pragma unroll
+                for (int l = 0; l < kDigits; ++l) bf[l][s][half] = pack_h2(e[l][0], e[l][1]);
+            }
+        }
+    }
+    // A-fragment offsets (halves) inside a slice plane for this lane: element
+    // (M row = block column g or g+8, K index kk) sits at window (r, j),
+    // kk = 10r + j, i.e. plane position (r, 4*block + j).
+    int aoff[5][2];
+#pragma unroll
+    for (int s = 0; s < 5; ++s)
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int kk = 16 * s + 2 * t + 8 * half;
+            const int r = kk / 10, j = kk - 10 * r;
+            aoff[s][half] = r * SL_PITCH + 4 * g + j;
+        }
+
+    constexpr int PAIRS = SL_X / 2;  // 35 column pairs per tile row
+    constexpr int NPAIR = SL_Y * PAIRS;
+    constexpr int PER = (NPAIR + 255) / 256;
+
+#pragma unroll 1
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+        const int x0 = tx * MT_X, y0 = ty * MT_Y;
+
+        // 1. Load the tile (pairs of columns) and its max |hi|.
+        float2 v0[PER], v1[PER];
+        float vmax = 0.f;
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int idx = tid + q * 256;
+            v0[q] = v1[q] = make_float2(0.f, 0.f);
+            if (idx < NPAIR) {
+                const int sy = idx / PAIRS, px = idx - sy * PAIRS;
+                const int gy = y0 - 3 + sy, gx = x0 - 3 + 2 * px;
+                if (gy < m + 3) {
+                    const float2 *row = in + (long long)gy * ld;
+                    if (gx < n + 3) v0[q] = row[gx];
+                    if (gx + 1 < n + 3) v1[q] = row[gx + 1];
+                }
+                vmax = fmaxf(vmax, fmaxf(fabsf(v0[q].x), fabsf(v1[q].x)));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        __syncthreads();  // previous tile's MMA phase is done with `sl` and `red`
+        if (lane == 0) red[warp] = vmax;
+        __syncthreads();
+        vmax = red[0];
+#pragma unroll
+        for (int i = 1; i < 8; ++i) vmax = fmaxf(vmax, red[i]);
+        int ex = 0;
+        if (vmax > 0.f) {
+            frexpf(vmax, &ex);  // vmax < 2^ex
+            ex += 1;            // |x| / 2^ex < 1/2
+        }
+        // 2. Slice into the digit planes.
+        const float to_digits = ldexpf(1.0f, kDigitBits - ex);
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int idx = tid + q * 256;
+            if (idx < NPAIR) {
+                const int sy = idx / PAIRS, px = idx - sy * PAIRS;
+                float d0[kDigits], d1[kDigits];
+                slice_digits(v0[q].x * to_digits, v0[q].y * to_digits, d0);
+                slice_digits(v1[q].x * to_digits, v1[q].y * to_digits, d1);
+                unsigned *dst = reinterpret_cast<unsigned *>(&sl[0][sy * SL_PITCH + 2 * px]);
+#pragma unroll
+                for (int k = 0; k < kDigits; ++k) dst[k * (SL_PLANE / 2)] = pack_h2(d0[k], d1[k]);
+            }
+        }
+        __syncthreads();
+
+        // 3. Two M-tiles (block rows) per warp.
+        const float out_scale = ldexpf(1.0f, ex + sw.ew - 2 * kDigitBits);
+#pragma unroll 1
+        for (int mt = 0; mt < 2; ++mt) {
+            const int br = warp * 2 + mt;  // block row: output rows 2br, 2br+1
+            float acc[kDigits][4];         // one exact accumulator per level k + l
+#pragma unroll
+            for (int lv = 0; lv < kDigits; ++lv) acc[lv][0] = acc[lv][1] = acc[lv][2] = acc[lv][3] = 0.f;
+            const int rowbase = (2 * br) * SL_PITCH;
+#pragma unroll
+            for (int s = 0; s < 5; ++s) {
+                unsigned af[kDigits][4];
+#pragma unroll
+                for (int k = 0; k < kDigits; ++k) {
+                    const __half *plane = sl[k] + rowbase;
+                    af[k][0] = *reinterpret_cast<const unsigned *>(plane + aoff[s][0]);
+                    af[k][1] = *reinterpret_cast<const unsigned *>(plane + aoff[s][0] + 32);
+                    af[k][2] = *reinterpret_cast<const unsigned *>(plane + aoff[s][1]);
+                    af[k][3] = *reinterpret_cast<const unsigned *>(plane + aoff[s][1] + 32);
+                }
+#pragma unroll
+                for (int lv = 0; lv < kDigits; ++lv)
+#pragma unroll
+                    for (int k = 0; k <= lv; ++k) mma16816(acc[lv], af[k], bf[lv - k][s][0], bf[lv - k][s][1]);
+            }
+            // 4. Recombine T = sum_lv acc[lv] * 2^(-9 lv) (levels 0..2 through
+            //    error-free sums; levels 3, 4 are below 2^-27 of level 0), and
+            //    y = T * 2^(ex + ew - 18).
+            float2 res[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float h1, e1, h2, e2, hi, lo;
+                two_sum(acc[0][c], acc[1][c] * 0x1p-9f, h1, e1);
+                two_sum(h1, acc[2][c] * 0x1p-18f, h2, e2);
+                const float tail = fmaf(acc[3][c], 0x1p-27f, acc[4][c] * 0x1p-36f);
+                two_sum(h2, (e1 + e2) + tail, hi, lo);
+                res[c] = make_float2(hi * out_scale, lo * out_scale);
+            }
+            // C fragment: c0,c1 -> block g, outputs n = 2t, 2t+1; c2,c3 -> block g+8.
+            const int yy = y0 + 2 * br + (t >> 1);
+#pragma unroll
+            for (int hb = 0; hb < 2; ++hb) {
+                const int xx = x0 + 4 * (g + 8 * hb) + 2 * (t & 1);
+                if (yy < m) {
+                    float2 *o = out + (long long)yy * ld + xx;
+                    if (xx + 1 < n) {
+                        *reinterpret_cast<float4 *>(o) = make_float4(res[2 * hb].x, res[2 * hb].y,
+                                                                     res[2 * hb + 1].x, res[2 * hb + 1].y);
+                    } else if (xx < n) {
+                        o[0] = res[2 * hb];
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ conversions
 __global__ void k_from_fp64(const double *__restrict__ src, float2 *__restrict__ dst, long long n)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -24,38 +445,182 @@ __global__ void k_to_fp64(const float2 *__restrict__ src, double *__restrict__ d
     }
 }
 
+// Re-anchor: round each (hi, lo) through FP64 back to a normalised pair.
+__global__ void k_reanchor(float2 *__restrict__ g, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = g[i];
+        const double x = (double)v.x + (double)v.y;
+        const float hi = __double2float_rn(x);
+        g[i] = make_float2(hi, __double2float_rn(x - (double)hi));
+    }
+}
+
 unsigned grid_for(long long n)
 {
     long long b = (n + 255) / 256;
     return (unsigned)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
 }
 
+unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+template <int K>
+FW<K> pack_ff(const Weights &w)
+{
+    FW<K> p;
+    for (int i = 0; i < K; ++i) {
+        const float h = (float)w.v[i];
+        p.hi[i] = h;
+        p.lo[i] = (float)(w.v[i] - (double)h);
+    }
+    return p;
+}
+
+template <int R>
+cudaError_t go1d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
+{
+    k1d_ff<R><<<ceil_div(g.ext[0], 1024), 256, 0, st>>>(in, out, g.ext[0], pack_ff<2 * R + 1>(w));
+    return cudaGetLastError();
+}
+
+template <int R, int P>
+cudaError_t go2d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
+{
+    constexpr int K = 2 * R + 1;
+    dim3 grid(ceil_div(g.ext[1], 64), ceil_div(g.ext[0], 32));
+    k2d_ff<R, P><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0],
+                                        pack_ff<K * K>(w));
+    return cudaGetLastError();
+}
+
+template <int R, int P>
+cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
+{
+    constexpr int K = 2 * R + 1;
+    constexpr int smem = K * (16 + 2 * R) * (32 + 2 * R) * (int)sizeof(float2);
+    static_assert(smem <= 48 * 1024, "3D ring exceeds the default shared-memory window");
+    const int zc = 32;
+    dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
+    k3d_ff<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
+                                           g.pitch[1], g.pitch[0], zc, pack_ff<K * K * K>(w));
+    return cudaGetLastError();
+}
+
+// Host: balanced base-512 digits of w / 2^ew (exact in double).
+SliceWeights slice_weights(const Weights &w)
+{
+    SliceWeights s{};
+    double mx = 0.0;
+    for (int i = 0; i < 49; ++i) mx = fmax(mx, fabs(w.v[i]));
+    int e = 0;
+    if (mx > 0.0) {
+        frexp(mx, &e);  // mx < 2^e
+        e += 1;
+    }
+    s.ew = e;
+    for (int i = 0; i < 49; ++i) {
+        double a = ldexp(w.v[i], kDigitBits - e);
+        for (int k = 0; k < kDigits; ++k) {  // balanced digits, |d| <= 256
+            const double d = rint(a);
+            s.d[k][i] = __float2half_rn((float)d);
+            a = (a - d) * (double)kRadix;
+        }
+    }
+    return s;
+}
+
 }  // namespace
 
-cudaError_t launch_split_from_fp64(const GridView &g, int, const double *src, float2 *dst,
-                                   cudaStream_t st)
+bool split_supported(int dims, int radius, int pattern)
+{
+    if (dims == 1) return radius >= 1 && radius <= 4;
+    if (dims == 2) return radius >= 1 && radius <= 3;
+    if (dims == 3) return radius == 1 || radius == 3;
+    return false;
+}
+
+bool split_mma_layout_ok(const GridView &g, long long origin)
+{
+    // float4 stores need even element offsets; the tile reads 3 halo columns.
+    return g.dims == 2 && (origin % 2) == 0 && (g.pitch[0] % 2) == 0;
+}
+
+cudaError_t launch_split_sweep(const GridView &g, int R, int P, const Weights &w, int algo_mma,
+                               const float2 *in, float2 *out, cudaStream_t st)
 {
     note_launch();
-    k_from_fp64<<<grid_for(g.ext[0]), 256, 0, st>>>(src, dst, g.ext[0]);
+    if (algo_mma) {
+        const int tiles_x = (int)ceil_div(g.ext[1], MT_X);
+        const int tiles = tiles_x * (int)ceil_div(g.ext[0], MT_Y);
+        const int grid = std::min(tiles, 2 * sm_count());
+        k2d_mma<<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0], tiles_x,
+                                      tiles, slice_weights(w));
+        return cudaGetLastError();
+    }
+    if (g.dims == 1) {
+        switch (R) {
+        case 1: return go1d<1>(g, w, in, out, st);
+        case 2: return go1d<2>(g, w, in, out, st);
+        case 3: return go1d<3>(g, w, in, out, st);
+        case 4: return go1d<4>(g, w, in, out, st);
+        }
+    } else if (g.dims == 2) {
+        if (R == 1) {
+            if (P == PAT_STAR) return go2d<1, PAT_STAR>(g, w, in, out, st);
+            return go2d<1, PAT_DENSE>(g, w, in, out, st);
+        }
+        if (R == 2) {
+            if (P == PAT_STAR) return go2d<2, PAT_STAR>(g, w, in, out, st);
+            if (P == PAT_DIAMOND) return go2d<2, PAT_DIAMOND>(g, w, in, out, st);
+            return go2d<2, PAT_DENSE>(g, w, in, out, st);
+        }
+        if (R == 3) {
+            if (P == PAT_STAR) return go2d<3, PAT_STAR>(g, w, in, out, st);
+            if (P == PAT_DIAMOND) return go2d<3, PAT_DIAMOND>(g, w, in, out, st);
+            return go2d<3, PAT_DENSE>(g, w, in, out, st);
+        }
+    } else if (g.dims == 3) {
+        if (R == 1) {
+            if (P == PAT_STAR) return go3d<1, PAT_STAR>(g, w, in, out, st);
+            return go3d<1, PAT_DENSE>(g, w, in, out, st);
+        }
+        if (R == 3) {
+            if (P == PAT_STAR) return go3d<3, PAT_STAR>(g, w, in, out, st);
+            if (P == PAT_DIAMOND) return go3d<3, PAT_DIAMOND>(g, w, in, out, st);
+            return go3d<3, PAT_DENSE>(g, w, in, out, st);
+        }
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_split_from_fp64(long long n, const double *src, float2 *dst, cudaStream_t st)
+{
+    note_launch();
+    k_from_fp64<<<grid_for(n), 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_to_fp64(const GridView &g, int, const float2 *src, double *dst,
-                                 cudaStream_t st)
+cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cudaStream_t st)
 {
     note_launch();
-    k_to_fp64<<<grid_for(g.ext[0]), 256, 0, st>>>(src, dst, g.ext[0]);
+    k_to_fp64<<<grid_for(n), 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
 
-bool split_supported(int, int, int) { return false; }
-
-cudaError_t launch_split_sweep(const GridView &, int, int, const Weights &, int, const float2 *,
-                               float2 *, cudaStream_t)
+cudaError_t launch_split_reanchor(long long n, float2 *grid, cudaStream_t st)
 {
-    return cudaErrorNotSupported;
+    note_launch();
+    k_reanchor<<<grid_for(n), 256, 0, st>>>(grid, n);
+    return cudaGetLastError();
 }
-
-cudaError_t launch_split_reanchor(const GridView &, float2 *, cudaStream_t) { return cudaSuccess; }
 
 }  // namespace cs

@@ -66,25 +66,29 @@ typedef enum cs_semantics { CS_SEM_STEP = 0, CS_SEM_FUSED = 1 } cs_semantics;
 
 /* Arithmetic of the sweep.
  * CS_PREC_FP64 : FP64 grids, FP64 arithmetic (FP64 FMA or FP64 MMA).
- * CS_PREC_SPLIT: grids stored as FP32 (hi, lo) pairs (8 bytes per point);
- *                the contraction runs on BF16 tensor cores over exact
- *                fixed-point slices with FP32 accumulation; see
- *                CS_OPT_SPLIT_LEVELS for the accuracy/speed trade. */
+ * CS_PREC_SPLIT: grids stored as FP32 (hi, lo) pairs (8 bytes per point,
+ *                about 48 significant bits); no FP64 arithmetic in the sweep.
+ *                Dense 7x7 kernels contract exact 10-bit fixed-point slices
+ *                on FP16 tensor cores (FP32 accumulation is exact for them);
+ *                other kernels use double-float FP32 arithmetic. Relative
+ *                error per sweep ~1e-13. Inputs must be finite. */
 typedef enum cs_precision { CS_PREC_FP64 = 0, CS_PREC_SPLIT = 1 } cs_precision;
 
 /* Kernel family; CS_ALGO_AUTO lets the plan's tuner choose. */
 typedef enum cs_algo {
     CS_ALGO_AUTO = 0,
-    CS_ALGO_FP64_FMA = 1, /* FP64 FMA, one output per tap-FMA (fewest FP64 ops) */
-    CS_ALGO_FP64_MMA = 2, /* FP64 tensor-core MMA (mma.sync m8n8k4.f64), 2x4 output blocks */
-    CS_ALGO_SPLIT_MMA = 3 /* split precision on BF16 tensor cores */
+    CS_ALGO_FP64_FMA = 1,  /* FP64 FMA, one FMA per non-zero tap (fewest FP64 ops) */
+    CS_ALGO_FP64_MMA = 2,  /* FP64 tensor-core MMA (mma.sync m8n8k4.f64), 2x4 output blocks;
+                              2D dense radius-3 kernels */
+    CS_ALGO_SPLIT_MMA = 3, /* split precision: exact 10-bit fixed-point slices on FP16
+                              tensor cores (mma.sync m16n8k16), 2D dense radius-3 kernels */
+    CS_ALGO_SPLIT_FMA = 4  /* split precision: double-float arithmetic on FP32 cores */
 } cs_algo;
 
 typedef enum cs_option {
-    CS_OPT_ALGO = 0,             /* cs_algo */
-    CS_OPT_SPLIT_LEVELS = 1,     /* 2..7 slice levels (default 5: <= 1e-10 rel.) */
-    CS_OPT_REANCHOR_INTERVAL = 2,/* split: renormalise (hi,lo) in FP64 every N steps (default 100, 0 = never) */
-    CS_OPT_TIME_BLOCK = 3        /* steps fused per launch by temporal blocking (0 = tuner) */
+    CS_OPT_ALGO = 0,              /* cs_algo */
+    CS_OPT_REANCHOR_INTERVAL = 2  /* split: renormalise (hi,lo) through FP64 every N
+                                     sweeps (default 100, 0 = never) */
 } cs_option;
 
 /* Where a grid lives in a buffer. extent/pitch are slowest axis first; the

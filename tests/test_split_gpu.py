@@ -1,0 +1,142 @@
+"""Split precision (FP32 hi+lo grids) on the GPU, through the C ABI.
+
+Bar: max pointwise relative error (denominator floored at 1e-3*max|ref|)
+<= 1e-10 against the FP64 CPU oracle, for every shape, both split kernels
+(FP16 tensor-core slices, double-float FP32) and ragged sizes.
+"""
+import numpy as np
+import pytest
+
+import convstencil_gb300 as cs
+from oracle import cs_oracle as O
+from tests.util import rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    cs.build()
+    O.build()
+
+
+def _dense(shape, w):
+    if shape == "star2d1r":
+        return O.star2d1r_to_dense(w)
+    if shape == "star2d3r":
+        return O.star2d3r_to_dense(w)
+    if shape == "star3d1r":
+        return O.star3d1r_to_dense(w)
+    return np.asarray(w, np.float64)
+
+
+def oracle_run(plan, buf, w_dense, r, steps):
+    L = plan.layout.as_dict()
+    ext = L["extent"]
+    o = L["origin"]
+    if L["dims"] == 1:
+        return O.run_1d(buf, w_dense, r, ext[0], o, steps)
+    if L["dims"] == 2:
+        ld = L["pitch"][0]
+        return O.run_2d(buf.reshape(-1, ld), w_dense, r, ext[0], ext[1], o // ld, o % ld,
+                        steps).reshape(-1)
+    lz, ly = L["pitch"][0], L["pitch"][1]
+    b3 = buf.reshape(-1, lz // ly, ly)
+    return O.run_3d(b3, w_dense, r, ext[0], ext[1], ext[2], o // lz, (o % lz) // ly, o % ly,
+                    steps).reshape(-1)
+
+
+def split_run(plan, host_fp64, steps):
+    """FP64 host buffer -> split device grid -> `steps` sweeps -> FP64 host."""
+    raw = torch.from_numpy(host_fp64).cuda()
+    a = torch.zeros(plan.elements * 2, dtype=torch.float32, device="cuda")
+    b = torch.zeros_like(a)
+    plan.split_from_fp64(raw, a)
+    in_b = plan.run(a, b, steps)
+    out = torch.zeros_like(raw)
+    plan.split_to_fp64(b if in_b else a, out)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+CASES = [
+    ("1d1r", (4099,), 9), ("1d2r", (2050,), 6),
+    ("star2d1r", (131, 197), 9), ("box2d1r", (64, 130), 5), ("star2d3r", (77, 65), 4),
+    ("box2d3r", (100, 129), 4), ("box2d3r", (64, 128), 3), ("box2d3r", (1, 1), 2),
+    ("box2d3r", (33, 70), 5),
+    ("star3d1r", (33, 20, 45), 4), ("box3d1r", (17, 35, 40), 3),
+]
+
+
+@pytest.mark.parametrize("shape,ext,steps", CASES)
+@pytest.mark.parametrize("algo", [cs.Algo.AUTO, cs.Algo.SPLIT_FMA, cs.Algo.SPLIT_MMA])
+def test_split_step_vs_oracle(shape, ext, steps, algo):
+    info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
+    w = O.seeded_weights(info[1], 500 + info[1])
+    p = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT)
+    try:
+        p.set_option(cs.Option.ALGO, algo)
+    except cs.ConvStencilError as e:
+        assert e.status == 2 and algo == cs.Algo.SPLIT_MMA
+        pytest.skip("tensor-core split kernel serves 2D radius-3 plans of at least 8x8")
+    x = O.splitmix_uniform(int(np.prod(ext)), 91).reshape(ext)
+    buf = p.pack(x)
+    got = split_run(p, buf, steps)
+    ref = oracle_run(p, buf, _dense(shape, w), info[4], steps)
+    err = rel_err(p.unpack(got), p.unpack(ref))
+    assert err[0] <= TOL, err
+
+
+@pytest.mark.parametrize("algo", [cs.Algo.SPLIT_FMA, cs.Algo.SPLIT_MMA])
+def test_split_fused_2d_kernels(algo):
+    """The reference's fused 7x7 kernels (cube of a 3x3 box, diamond of a star)."""
+    for base, dense in ((O.seeded_weights(9, 3), None), (O.seeded_weights(5, 4), "star")):
+        w49 = O.selfconv(O.star2d1r_to_dense(base) if dense else base, 2, 1, 3)
+        ext = (70, 90)
+        p = cs.Plan("box2d3r", ext, w49, semantics=cs.Semantics.FUSED, precision=cs.Precision.SPLIT)
+        p.set_option(cs.Option.ALGO, algo)
+        x = O.splitmix_uniform(ext[0] * ext[1], 8).reshape(ext)
+        buf = p.pack(x)
+        got = split_run(p, buf, 3)
+        ref = oracle_run(p, buf, w49, 3, 3)
+        assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
+def test_split_signed_weights_and_wide_range():
+    """Mixed-sign weights and inputs spanning many binades per tile."""
+    ext = (96, 130)
+    w = O.seeded_weights(49, 12) - 1.0 / 49 * 0.5
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(ext) * np.exp(rng.uniform(-8, 8, ext))
+    for algo in (cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_FMA):
+        p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+        p.set_option(cs.Option.ALGO, algo)
+        buf = p.pack(x)
+        got = split_run(p, buf, 2)
+        ref = oracle_run(p, buf, w, 3, 2)
+        # normwise bar: values span 14 binades inside a tile
+        assert rel_err(p.unpack(got), p.unpack(ref))[1] <= TOL
+
+
+def test_split_long_run_with_reanchor():
+    ext = (128, 192)
+    w = O.seeded_weights(49, 21)
+    p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.REANCHOR_INTERVAL, 25)
+    x = O.splitmix_uniform(ext[0] * ext[1], 22).reshape(ext)
+    buf = p.pack(x)
+    got = split_run(p, buf, 200)
+    ref = oracle_run(p, buf, w, 3, 200)
+    err = rel_err(p.unpack(got), p.unpack(ref))
+    assert err[1] <= TOL and err[0] <= 1e-8, err
+
+
+def test_split_roundtrip_conversion():
+    p = cs.Plan("box2d3r", (40, 50), O.seeded_weights(49, 1), precision=cs.Precision.SPLIT)
+    x = O.splitmix_uniform(40 * 50, 5).reshape(40, 50) * 1e3 - 400.0
+    buf = p.pack(x)
+    got = split_run(p, buf, 0)
+    np.testing.assert_allclose(got, buf, rtol=2.0 ** -47, atol=0)
