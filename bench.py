@@ -181,6 +181,39 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------ ncu cases
+def run_kernel_case(args):
+    """One box2d3r plan, one algorithm, `sweeps` sweeps on an m x n grid."""
+    import torch
+    import convstencil_gb300 as cs
+    from oracle import cs_oracle as O
+    m, n = args.m, args.n
+    x = O.splitmix_uniform(m * n, GRID_SEED).reshape(m, n)
+    w = O.seeded_weights(TAPS, WEIGHT_SEED)
+    algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA,
+            "split_mma": cs.Algo.SPLIT_MMA, "split_fma": cs.Algo.SPLIT_FMA}[args.kernel_case]
+    split = args.kernel_case.startswith("split")
+    p = cs.Plan(SHAPE, (m, n), w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
+    p.set_option(cs.Option.ALGO, algo)
+    host = torch.from_numpy(p.pack(x)).cuda()
+    if split:
+        a = torch.zeros(p.elements * 2, dtype=torch.float32, device="cuda")
+        p.split_from_fp64(host, a)
+    else:
+        a = host
+    b = torch.zeros_like(a)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    p.run(a, b, args.sweeps)
+    ev1.record()
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / max(1, args.sweeps)
+    print(json.dumps({"kernel_case": args.kernel_case, "m": m, "n": n, "sweeps": args.sweeps,
+                      "ms_per_sweep": round(ms, 4), "gstencil_s": round(m * n / ms / 1e6, 3)}))
+    return 0
+
+
 # ---------------------------------------------------------------------- ours
 def main():
     ap = argparse.ArgumentParser()
@@ -191,9 +224,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--kernel-case", default=None,
+                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_fma"],
+                    help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid "
+                         "(small cases for ncu captures) and exit")
+    ap.add_argument("--m", type=int, default=4608)
+    ap.add_argument("--n", type=int, default=4608)
+    ap.add_argument("--sweeps", type=int, default=4)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_case:
+        return run_kernel_case(args)
     args.warmup = max(3, args.warmup)
 
     import torch

@@ -76,6 +76,7 @@ class Algo(enum.IntEnum):
     FP64_MMA = 2
     SPLIT_MMA = 3
     SPLIT_FMA = 4
+    SPLIT_MMA_TMA = 5
 
 
 class Option(enum.IntEnum):
@@ -139,6 +140,7 @@ def lib() -> ctypes.CDLL:
     L.cs_last_loop_seconds.restype = ctypes.c_double
     L.cs_kernel_launch_count.restype = ctypes.c_longlong
     L.cs_version.restype = ctypes.c_char_p
+    L.cs_device_wait_timeouts.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
     _lib = L
     return L
 
@@ -156,6 +158,13 @@ def kernel_launch_count() -> int:
 
 def last_loop_seconds() -> float:
     return float(lib().cs_last_loop_seconds())
+
+
+def device_wait_timeouts(reset: bool = True) -> int:
+    """Bounded device-side waits that expired (0 in a healthy run)."""
+    c = ctypes.c_uint()
+    check(lib().cs_device_wait_timeouts(ctypes.byref(c), 1 if reset else 0))
+    return int(c.value)
 
 
 def set_verbose(on: bool) -> None:

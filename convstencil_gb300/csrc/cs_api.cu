@@ -248,6 +248,10 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(p->view, p->w, in, out, st);
         return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st);
     }
+    if (algo == CS_ALGO_SPLIT_MMA_TMA && cs::split_tma_layout_ok(p->view, off, in_base))
+        return cs::launch_split_sweep_tma(p->view, p->w, off, p->layout.elements,
+                                          (const float2 *)in_base, (float2 *)out_base, st);
+    if (algo == CS_ALGO_SPLIT_MMA_TMA) algo = CS_ALGO_SPLIT_MMA;  // buffer not TMA-aligned
     const float2 *in = (const float2 *)in_base + off;
     float2 *out = (float2 *)out_base + off;
     return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, algo == CS_ALGO_SPLIT_MMA,
@@ -272,18 +276,16 @@ int size_class(const cs_plan *p)
 // no result) and the winner is remembered for plans of the same class.
 cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *out)
 {
-    int cand[2];
+    int cand[3];
+    int nc = 0;
     if (p->prec == CS_PREC_SPLIT) {
-        if (p->algo == CS_ALGO_SPLIT_FMA || !split_mma_ok(p)) {
-            *out = CS_ALGO_SPLIT_FMA;
+        if (p->algo != CS_ALGO_AUTO || !split_mma_ok(p)) {
+            *out = split_mma_ok(p) ? p->algo : CS_ALGO_SPLIT_FMA;
             return CS_OK;
         }
-        if (p->algo == CS_ALGO_SPLIT_MMA) {
-            *out = CS_ALGO_SPLIT_MMA;
-            return CS_OK;
-        }
-        cand[0] = CS_ALGO_SPLIT_MMA;
-        cand[1] = CS_ALGO_SPLIT_FMA;
+        cand[nc++] = CS_ALGO_SPLIT_MMA;
+        cand[nc++] = CS_ALGO_SPLIT_MMA_TMA;
+        cand[nc++] = CS_ALGO_SPLIT_FMA;
     } else {
         if (p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) {
             *out = CS_ALGO_FP64_MMA;
@@ -293,8 +295,8 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
             *out = CS_ALGO_FP64_FMA;
             return CS_OK;
         }
-        cand[0] = CS_ALGO_FP64_FMA;
-        cand[1] = CS_ALGO_FP64_MMA;
+        cand[nc++] = CS_ALGO_FP64_FMA;
+        cand[nc++] = CS_ALGO_FP64_MMA;
     }
     auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
     {
@@ -311,7 +313,8 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
     CS_CUDA(cudaEventCreate(&e0));
     CS_CUDA(cudaEventCreate(&e1));
     for (int rep = 0; rep < 2; ++rep) {  // rep 0 warms up
-        for (int c : cand) {
+        for (int ci = 0; ci < nc; ++ci) {
+            const int c = cand[ci];
             CS_CUDA(cudaEventRecord(e0, st));
             CS_CUDA(launch_sweep(p, c, a, b, st));
             CS_CUDA(cudaEventRecord(e1, st));
@@ -357,6 +360,13 @@ CS_API void cs_set_verbose(int on) { g_verbose.store(on); }
 CS_API double cs_last_loop_seconds(void) { return t_loop_seconds; }
 CS_API long long cs_kernel_launch_count(void) { return cs::g_launches.load(); }
 CS_API const char *cs_version(void) { return "convstencil_gb300 0.1 (sm_103a)"; }
+
+CS_API cs_status cs_device_wait_timeouts(unsigned *count, int reset)
+{
+    if (!count) return fail(CS_ERR_INVALID_ARGUMENT, "count is NULL");
+    CS_CUDA(cs::split_wait_timeouts(count, reset != 0));
+    return CS_OK;
+}
 
 CS_API cs_status cs_plan_create(cs_plan **out, cs_shape shape, cs_semantics sem, cs_precision prec,
                                 const long long *extent, const double *weights, int n_weights,
@@ -427,14 +437,15 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
     if (!p) return fail(CS_ERR_INVALID_ARGUMENT, "plan is NULL");
     switch (opt) {
     case CS_OPT_ALGO:
-        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_FMA) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
-        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_FMA) && p->prec != CS_PREC_SPLIT)
+        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_MMA_TMA) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
+        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_FMA || v == CS_ALGO_SPLIT_MMA_TMA) &&
+            p->prec != CS_PREC_SPLIT)
             return fail(CS_ERR_INVALID_ARGUMENT, "split algo needs a split-precision plan");
         if ((v == CS_ALGO_FP64_FMA || v == CS_ALGO_FP64_MMA) && p->prec != CS_PREC_FP64)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
         if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
-        if (v == CS_ALGO_SPLIT_MMA && !split_mma_ok(p))
+        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_MMA_TMA) && !split_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
                         "split MMA serves 2D radius-3 plans of at least 8x8 on even-aligned layouts");
         p->algo = (int)v;

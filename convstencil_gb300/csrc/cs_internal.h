@@ -48,6 +48,15 @@ cudaError_t launch_split_sweep(const GridView &g, int radius, int pattern, const
                                int use_mma, const float2 *in, float2 *out, cudaStream_t stream);
 bool split_supported(int dims, int radius, int pattern);
 bool split_mma_layout_ok(const GridView &g, long long origin);
+// Warp-specialised TMA variant of the slice kernel (cs_kernels_split_tma.cu);
+// needs an even row pitch, >= 4 halo columns left of the interior (the TMA box
+// starts 16-byte aligned at x0-4), >= 3 halo rows, and a 16-byte aligned base.
+bool split_tma_layout_ok(const GridView &g, long long origin, const void *base);
+cudaError_t launch_split_sweep_tma(const GridView &g, const Weights &w, long long origin,
+                                   long long elements, const float2 *in_base, float2 *out_base,
+                                   cudaStream_t stream);
+// Bounded device-side waits that expired since the last reset.
+cudaError_t split_wait_timeouts(unsigned *count, bool reset);
 // Whole-buffer conversions and re-anchoring over n elements.
 cudaError_t launch_split_from_fp64(long long n, const double *src, float2 *dst, cudaStream_t stream);
 cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cudaStream_t stream);

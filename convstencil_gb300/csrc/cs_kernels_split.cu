@@ -25,27 +25,28 @@
 //    of a block, one MMA row per block, K = the 8x10 input window of a block
 //    (80 = 5 k-steps of 16).
 #include "cs_internal.h"
+#include "cs_split_common.cuh"
 
 #include <cuda_fp16.h>
 
 #include <algorithm>
 
 namespace cs {
-
-struct SplitWeights {
-    float hi[kMaxTaps];
-    float lo[kMaxTaps];
-};
-
 namespace {
 
-// ------------------------------------------------------- error-free pieces
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
+using split::kDigitBits;
+using split::kDigits;
+using split::MT_X;
+using split::MT_Y;
+using split::SL_PITCH;
+using split::SL_PLANE;
+using split::SL_X;
+using split::SL_Y;
+using split::SliceWeights;
+using split::mma16816;
+using split::pack_h2;
+using split::slice_digits;
+using split::two_sum;
 
 // One tap of a double-float dot product: (sh, sl) += (wh + wl) * (xh + xl).
 __device__ __forceinline__ void ff_tap(float &sh, float &sl, float wh, float wl, float xh, float xl)
@@ -208,62 +209,17 @@ __global__ void __launch_bounds__(256) k3d_ff(const float2 *__restrict__ in, flo
 }
 
 // ------------------------------------------------------- tensor-core form
-constexpr int kDigits = 5;       // x and w slices
-constexpr int kDigitBits = 9;    // balanced base-512 digits, |d| <= 256
-constexpr float kRadix = 512.f;
-
-struct SliceWeights {
-    __half d[kDigits][49];  // digits of w / 2^Ew, row-major 7x7
-    int ew;                 // weight scale exponent: |w| < 2^(ew-1)
-};
-
-__device__ __forceinline__ void mma16816(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ unsigned pack_h2(float lo_elem, float hi_elem)
-{
-    const __half2 h = __floats2half2_rn(lo_elem, hi_elem);  // .x = first (lower address)
-    return *reinterpret_cast<const unsigned *>(&h);
-}
-
-// Cuts x' = (a + b) (|x'| < 256 after the first scaling) into five balanced
-// base-512 digits. Every step is exact: rint(a) is an integer within 1/2 of
-// a, a - rint(a) is representable, and two_sum keeps (a, b) normalised.
-__device__ __forceinline__ void slice_digits(float a, float b, float (&d)[kDigits])
-{
-#pragma unroll
-    for (int k = 0; k < kDigits - 1; ++k) {
-        d[k] = rintf(a);
-        float s, e;
-        two_sum(a - d[k], b, s, e);
-        a = s * kRadix;
-        b = e * kRadix;
-    }
-    d[kDigits - 1] = rintf(a + b);
-}
-
-constexpr int MT_X = 64, MT_Y = 32;              // CTA output tile
-constexpr int SL_X = MT_X + 6, SL_Y = MT_Y + 6;  // input tile with radius-3 halo
-// Halves per slice row. 102 halves = 51 words = 19 mod 32 banks: when the
-// K indices of one A-fragment load straddle two window rows, the two rows'
-// words land in disjoint banks.
-constexpr int SL_PITCH = 102;
-constexpr int SL_PLANE = SL_Y * SL_PITCH;
-
 // Persistent: each CTA walks tiles tile = blockIdx.x, +gridDim.x, ...; the
-// weight digits are staged in shared memory and turned into B fragments once.
-__global__ void __launch_bounds__(256, 2) k2d_mma(const float2 *__restrict__ in,
+// weight digits are turned into per-lane B fragments once per CTA and kept in
+// shared memory (one conflict-free LDS.64 per digit and k-step), which leaves
+// registers for three resident CTAs per SM.
+__global__ void __launch_bounds__(256, 3) k2d_mma(const float2 *__restrict__ in,
                                                   float2 *__restrict__ out, int m, int n,
                                                   long long ld, int tiles_x, int tiles,
                                                   SliceWeights sw)
 {
     __shared__ __align__(16) __half sl[kDigits][SL_PLANE];
+    __shared__ __align__(16) uint2 bsm[kDigits][5][32];
     __shared__ __half wd[kDigits * 49];
     __shared__ float red[8];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -271,30 +227,26 @@ __global__ void __launch_bounds__(256, 2) k2d_mma(const float2 *__restrict__ in,
 
     for (int i = tid; i < kDigits * 49; i += blockDim.x) wd[i] = sw.d[i / 49][i % 49];
     __syncthreads();
-    // B fragments (weights' digits) for this lane: column n = g of the 2x4
+    // B fragments (weights' digits) for lane (g, t): column n = g of the 2x4
     // block (a = g/4, b = g%4), rows kk = 16s + {2t, 2t+1, 2t+8, 2t+9};
     // B[kk][n] = w[r-a][j-b] with kk = 10r + j.
-    unsigned bf[kDigits][5][2];
-    {
+    if (warp == 0) {
         const int a = g >> 2, b = g & 3;
-#pragma unroll
         for (int s = 0; s < 5; ++s) {
-#pragma unroll
+            unsigned reg[kDigits][2];
             for (int half = 0; half < 2; ++half) {
                 float e[kDigits][2];
-#pragma unroll
                 for (int u = 0; u < 2; ++u) {
                     const int kk = 16 * s + 2 * t + 8 * half + u;
                     const int r = kk / 10, j = kk - 10 * r;
                     const int ri = r - a, ci = j - b;
                     const bool in_w = ri >= 0 && ri < 7 && ci >= 0 && ci < 7;
-#pragma unroll
                     for (int l = 0; l < kDigits; ++l)
                         e[l][u] = in_w ? __half2float(wd[l * 49 + ri * 7 + ci]) : 0.f;
                 }
-#pragma unroll
-                for (int l = 0; l < kDigits; ++l) bf[l][s][half] = pack_h2(e[l][0], e[l][1]);
+                for (int l = 0; l < kDigits; ++l) reg[l][half] = pack_h2(e[l][0], e[l][1]);
             }
+            for (int l = 0; l < kDigits; ++l) bsm[l][s][lane] = make_uint2(reg[l][0], reg[l][1]);
         }
     }
     // A-fragment offsets (halves) inside a slice plane for this lane: element
@@ -387,10 +339,13 @@ __global__ void __launch_bounds__(256, 2) k2d_mma(const float2 *__restrict__ in,
                     af[k][2] = *reinterpret_cast<const unsigned *>(plane + aoff[s][1]);
                     af[k][3] = *reinterpret_cast<const unsigned *>(plane + aoff[s][1] + 32);
                 }
+                uint2 bf[kDigits];
+#pragma unroll
+                for (int l = 0; l < kDigits; ++l) bf[l] = bsm[l][s][lane];
 #pragma unroll
                 for (int lv = 0; lv < kDigits; ++lv)
 #pragma unroll
-                    for (int k = 0; k <= lv; ++k) mma16816(acc[lv], af[k], bf[lv - k][s][0], bf[lv - k][s][1]);
+                    for (int k = 0; k <= lv; ++k) mma16816(acc[lv], af[k], bf[lv - k].x, bf[lv - k].y);
             }
             // 4. Recombine T = sum_lv acc[lv] * 2^(-9 lv) (levels 0..2 through
             //    error-free sums; levels 3, 4 are below 2^-27 of level 0), and
@@ -515,29 +470,6 @@ cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *
     return cudaGetLastError();
 }
 
-// Host: balanced base-512 digits of w / 2^ew (exact in double).
-SliceWeights slice_weights(const Weights &w)
-{
-    SliceWeights s{};
-    double mx = 0.0;
-    for (int i = 0; i < 49; ++i) mx = fmax(mx, fabs(w.v[i]));
-    int e = 0;
-    if (mx > 0.0) {
-        frexp(mx, &e);  // mx < 2^e
-        e += 1;
-    }
-    s.ew = e;
-    for (int i = 0; i < 49; ++i) {
-        double a = ldexp(w.v[i], kDigitBits - e);
-        for (int k = 0; k < kDigits; ++k) {  // balanced digits, |d| <= 256
-            const double d = rint(a);
-            s.d[k][i] = __float2half_rn((float)d);
-            a = (a - d) * (double)kRadix;
-        }
-    }
-    return s;
-}
-
 }  // namespace
 
 bool split_supported(int dims, int radius, int pattern)
@@ -561,9 +493,9 @@ cudaError_t launch_split_sweep(const GridView &g, int R, int P, const Weights &w
     if (algo_mma) {
         const int tiles_x = (int)ceil_div(g.ext[1], MT_X);
         const int tiles = tiles_x * (int)ceil_div(g.ext[0], MT_Y);
-        const int grid = std::min(tiles, 2 * sm_count());
+        const int grid = std::min(tiles, 3 * sm_count());
         k2d_mma<<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0], tiles_x,
-                                      tiles, slice_weights(w));
+                                      tiles, split::slice_weights(w));
         return cudaGetLastError();
     }
     if (g.dims == 1) {

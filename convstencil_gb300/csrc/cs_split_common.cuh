@@ -1,0 +1,97 @@
+// cs_split_common.cuh — pieces shared by the split-precision kernels:
+// error-free FP32 transformations, the balanced-digit slicing of (hi, lo)
+// pairs and of the weights, and the FP16 mma.sync wrapper.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include <cmath>
+
+#include "cs_internal.h"
+
+namespace cs {
+namespace split {
+
+// s + e == a + b exactly (Knuth's TwoSum, no ordering requirement).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+constexpr int kDigits = 5;       // x and w slices
+constexpr int kDigitBits = 9;    // balanced base-512 digits, |d| <= 256
+constexpr float kRadix = 512.f;
+
+struct SliceWeights {
+    __half d[kDigits][49];  // digits of w / 2^Ew, row-major 7x7
+    int ew;                 // weight scale exponent: |w| < 2^(ew-1)
+};
+
+__device__ __forceinline__ void mma16816(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ unsigned pack_h2(float lo_elem, float hi_elem)
+{
+    const __half2 h = __floats2half2_rn(lo_elem, hi_elem);  // .x = first (lower address)
+    return *reinterpret_cast<const unsigned *>(&h);
+}
+
+// Cuts x' = (a + b) (|x'| < 256 after the first scaling) into five balanced
+// base-512 digits. Every step is exact: rint(a) is an integer within 1/2 of
+// a, a - rint(a) is representable, and two_sum keeps (a, b) normalised.
+__device__ __forceinline__ void slice_digits(float a, float b, float (&d)[kDigits])
+{
+#pragma unroll
+    for (int k = 0; k < kDigits - 1; ++k) {
+        d[k] = rintf(a);
+        float s, e;
+        two_sum(a - d[k], b, s, e);
+        a = s * kRadix;
+        b = e * kRadix;
+    }
+    d[kDigits - 1] = rintf(a + b);
+}
+
+constexpr int MT_X = 64, MT_Y = 32;              // CTA output tile
+constexpr int SL_X = MT_X + 6, SL_Y = MT_Y + 6;  // input tile with radius-3 halo
+// Halves per slice row. 102 halves = 51 words = 19 mod 32 banks: when the
+// K indices of one A-fragment load straddle two window rows, the two rows'
+// words land in disjoint banks.
+constexpr int SL_PITCH = 102;
+constexpr int SL_PLANE = SL_Y * SL_PITCH;
+
+
+// Balanced base-512 digits of w / 2^ew for the 49 taps (exact in double);
+// ew is chosen so that every |w| / 2^ew < 1/2.
+inline SliceWeights slice_weights(const Weights &w)
+{
+    SliceWeights s{};
+    double mx = 0.0;
+    for (int i = 0; i < 49; ++i) mx = std::fmax(mx, std::fabs(w.v[i]));
+    int e = 0;
+    if (mx > 0.0) {
+        std::frexp(mx, &e);  // mx < 2^e
+        e += 1;
+    }
+    s.ew = e;
+    for (int i = 0; i < 49; ++i) {
+        double a = std::ldexp(w.v[i], kDigitBits - e);
+        for (int k = 0; k < kDigits; ++k) {  // balanced digits, |d| <= 256
+            const double d = std::rint(a);
+            s.d[k][i] = __float2half_rn((float)d);
+            a = (a - d) * (double)kRadix;
+        }
+    }
+    return s;
+}
+
+}  // namespace split
+}  // namespace cs

@@ -82,7 +82,9 @@ typedef enum cs_algo {
                               2D dense radius-3 kernels */
     CS_ALGO_SPLIT_MMA = 3, /* split precision: exact 10-bit fixed-point slices on FP16
                               tensor cores (mma.sync m16n8k16), 2D dense radius-3 kernels */
-    CS_ALGO_SPLIT_FMA = 4  /* split precision: double-float arithmetic on FP32 cores */
+    CS_ALGO_SPLIT_FMA = 4, /* split precision: double-float arithmetic on FP32 cores */
+    CS_ALGO_SPLIT_MMA_TMA = 5 /* as CS_ALGO_SPLIT_MMA, warp-specialised: TMA tile loads and
+                                 slicing in producer warps, MMA in consumer warps */
 } cs_algo;
 
 typedef enum cs_option {
@@ -177,6 +179,11 @@ CS_API double cs_last_loop_seconds(void);
 CS_API long long cs_kernel_launch_count(void);
 /* Library version string. */
 CS_API const char *cs_version(void);
+/* Device-side waits (mbarrier waits in the pipelined kernels) are bounded;
+ * each one that expires is counted here instead of hanging the GPU. Reads
+ * the count (synchronous) and, if reset, clears it. A non-zero count means
+ * the affected sweeps' outputs are incomplete. */
+CS_API cs_status cs_device_wait_timeouts(unsigned *count, int reset);
 
 #ifdef __cplusplus
 }
