@@ -765,3 +765,52 @@ CS_API cs_status cs_gpu_star_3d1r(const double *in, double *out, const double *p
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Sweeps from a read-only input into an output through a caller-supplied
+// intermediate grid, with no allocation and no tuning run: the algorithm is
+// the one the tuner already chose for this plan's class, else the default.
+// Used by the no-allocation entry point (cs_noalloc.cu).
+namespace cs {
+
+size_t plan_bytes(const cs_plan *p) { return p->layout.bytes; }
+
+cs_status run_into(cs_plan *p, const void *in, void *out, void *scratch, long long steps,
+                   cudaStream_t st)
+{
+    long long sweeps = 0;
+    cs_status s = cs_plan_sweeps(p, steps, &sweeps);
+    if (s != CS_OK) return s;
+    if (sweeps == 0) {
+        CS_CUDA(cudaMemcpyAsync(out, in, p->layout.bytes, cudaMemcpyDeviceToDevice, st));
+        return CS_OK;
+    }
+    int algo;
+    if (p->prec == CS_PREC_SPLIT)
+        algo = p->algo != CS_ALGO_AUTO ? p->algo : (split_mma_ok(p) ? CS_ALGO_SPLIT_MMA : CS_ALGO_SPLIT_FMA);
+    else
+        algo = p->algo != CS_ALGO_AUTO ? p->algo : CS_ALGO_FP64_FMA;
+    if (p->algo == CS_ALGO_AUTO) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p)));
+        if (it != g_tune.end()) algo = it->second;
+    }
+    // The last sweep lands in `out`; earlier ones alternate so that sweep i
+    // writes `out` when (sweeps - i) is even and `scratch` otherwise.
+    const void *src = in;
+    for (long long i = 1; i <= sweeps; ++i) {
+        void *dst = ((sweeps - i) % 2 == 0) ? out : scratch;
+        cudaError_t e = launch_sweep(p, algo, src, dst, st);
+        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && (i % p->reanchor) == 0) {
+            e = launch_split_reanchor(p->layout.elements, (float2 *)dst, st);
+            if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
+        }
+        src = dst;
+    }
+    return CS_OK;
+}
+
+cs_status set_error(cs_status s, const char *msg) { return fail(s, "%s", msg); }
+
+}  // namespace cs

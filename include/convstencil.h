@@ -132,6 +132,26 @@ CS_API cs_status cs_plan_destroy(cs_plan *plan);
 CS_API cs_status cs_run(cs_plan *plan, void *a, void *b, long long steps, void *stream,
                         int *result_in_b);
 
+/* Runs `steps` steps from device buffer `in` into device buffer `out` (plan
+ * layout, zero halos) and allocates nothing: the intermediate grid of the
+ * ping-pong is a fixed 16 MiB array that this library reserves on every GPU
+ * that loads it, for the life of the process. `in` is left unchanged.
+ * No counterpart in the reference, whose wrappers always cudaMalloc.
+ * For callers that must not allocate device memory at this point: a host
+ * process whose framework allocator already holds the GPU's memory (a fresh
+ * cudaMalloc would fail or fragment it), or a latency-critical loop that
+ * cannot afford cudaMalloc's implicit device synchronisation.
+ * Limits: one buffer of the plan's layout must fit in 16 MiB (2,097,152
+ * points of 8 bytes); larger grids get CS_ERR_INVALID_ARGUMENT. The first
+ * call on each device looks up the array's device address (with that device
+ * current); make that first call before any stream capture. Every call shares
+ * the one array per device: calls whose work overlaps on the GPU (different
+ * streams, or threads) race on it and must be serialised by the caller.
+ * With CS_ALGO_AUTO it uses the kernel the tuner already chose for this kind
+ * of plan (else the default), and runs no tuning sweeps of its own. */
+CS_API cs_status cs_run_noalloc(cs_plan *plan, const void *in, void *out, long long steps,
+                                void *stream);
+
 /* Split precision: FP64 grid <-> (hi, lo) FP32 pairs, same layout. */
 CS_API cs_status cs_split_from_fp64(const cs_plan *plan, const double *src, void *dst, void *stream);
 CS_API cs_status cs_split_to_fp64(const cs_plan *plan, const void *src, double *dst, void *stream);
