@@ -97,6 +97,28 @@ class Layout(ctypes.Structure):
                 "elements": self.elements, "bytes": self.bytes}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("streams", ctypes.c_int), ("max_active", ctypes.c_int),
+                ("hbm_fraction", ctypes.c_double), ("chunk_steps", ctypes.c_longlong),
+                ("use_graphs", ctypes.c_int)]
+
+
+class RequestDesc(ctypes.Structure):
+    _fields_ = [("shape", ctypes.c_int), ("semantics", ctypes.c_int), ("precision", ctypes.c_int),
+                ("extent", ctypes.c_longlong * 3), ("weights", ctypes.POINTER(ctypes.c_double)),
+                ("n_weights", ctypes.c_int), ("interior_in", ctypes.POINTER(ctypes.c_double)),
+                ("steps", ctypes.c_longlong)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong),
+                ("queued", ctypes.c_longlong), ("active", ctypes.c_longlong),
+                ("hbm_budget_bytes", ctypes.c_longlong), ("hbm_reserved_bytes", ctypes.c_longlong),
+                ("p50_s", ctypes.c_double), ("p99_s", ctypes.c_double), ("mean_s", ctypes.c_double),
+                ("point_steps", ctypes.c_double), ("wall_s", ctypes.c_double),
+                ("gstencil_s", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -141,6 +163,11 @@ def lib() -> ctypes.CDLL:
     L.cs_kernel_launch_count.restype = ctypes.c_longlong
     L.cs_version.restype = ctypes.c_char_p
     L.cs_device_wait_timeouts.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
+    L.cs_server_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]
+    L.cs_server_submit.argtypes = [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ll)]
+    L.cs_server_wait.argtypes = [vp, ll, dp, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    L.cs_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.cs_server_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -309,6 +336,65 @@ def _layout_from_dict(d) -> Layout:
     return L
 
 
+# -------------------------------------------------------------- serving
+class Server:
+    """Continuous-batching stencil server (cs_server_* in convstencil.h).
+
+    ``submit`` copies a dense interior grid and returns an id at once; the
+    server's worker admits requests by free HBM, keeps them device-resident,
+    interleaves their sweeps on a pool of streams, and ``wait`` returns the
+    dense interior result and the request's latency."""
+
+    def __init__(self, streams=8, max_active=64, hbm_fraction=0.8, chunk_steps=32, use_graphs=True):
+        cfg = ServerConfig(streams, max_active, hbm_fraction, chunk_steps, 1 if use_graphs else 0)
+        h = ctypes.c_void_p()
+        check(lib().cs_server_create(ctypes.byref(h), ctypes.byref(cfg)))
+        self._h = h
+        self._shapes = {}
+
+    def submit(self, shape, interior, weights, steps, precision=Precision.FP64,
+               semantics=Semantics.STEP) -> int:
+        if isinstance(shape, str):
+            shape = SHAPE_BY_NAME[shape]
+        x = np.ascontiguousarray(interior, np.float64)
+        w = np.ascontiguousarray(np.asarray(weights, np.float64).reshape(-1))
+        ext = list(x.shape) + [1] * (3 - x.ndim)
+        d = RequestDesc(int(shape), int(semantics), int(precision), (ctypes.c_longlong * 3)(*ext),
+                        _dptr(w), int(w.size), _dptr(x), int(steps))
+        rid = ctypes.c_longlong()
+        check(lib().cs_server_submit(self._h, ctypes.byref(d), ctypes.byref(rid)))
+        self._shapes[int(rid.value)] = x.shape
+        return int(rid.value)
+
+    def wait(self, rid: int, timeout: float = 0.0):
+        out = np.empty(self._shapes.pop(rid), np.float64)
+        lat = ctypes.c_double()
+        check(lib().cs_server_wait(self._h, rid, _dptr(out), float(timeout), ctypes.byref(lat)))
+        return out, float(lat.value)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().cs_server_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cs_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------- reference-named wrappers
 def _host_args(inp, out, params, n_params):
     p = np.ascontiguousarray(params, np.float64).reshape(-1)
@@ -387,6 +473,6 @@ def selfconv(w, dims: int, r: int, k: int) -> np.ndarray:
     return acc.reshape(-1)
 
 
-__all__ = ["Plan", "Layout", "Shape", "Semantics", "Precision", "Algo", "Option",
+__all__ = ["Plan", "Server", "Layout", "Shape", "Semantics", "Precision", "Algo", "Option",
            "ConvStencilError", "gpu_1d1r", "gpu_star_1d2r_step2", "gpu_box_2d1r", "gpu_box_2d3r",
            "gpu_box_3d1r", "gpu_star_3d1r", "selfconv", "build", "lib", "kernel_launch_count"]

@@ -1,0 +1,526 @@
+// cs_serve.cu — a continuous-batching stencil server (C ABI in convstencil.h).
+//
+// Clients submit stencil solves (shape, grid, weights, steps, precision) from
+// any thread; a worker thread owns the GPU work:
+//   * admission: a request is admitted when its device buffers fit in the HBM
+//     budget (a share of the memory free at creation) and a slot is free; it
+//     then stays device-resident until its last step;
+//   * execution: every scheduling turn issues one chunk of sweeps per active
+//     request on that request's stream (a pool of streams), so the work of
+//     different requests overlaps on the device; a chunk is captured once as a
+//     CUDA graph and replayed;
+//   * completion: the result goes to a pinned host buffer, the device memory is
+//     released (making room for queued requests), the latency is recorded.
+// Kernel choice and FP64 re-anchoring points depend only on the request, never
+// on what else is running, so a request's result is bitwise identical alone
+// and in any mix.
+#include "../../include/convstencil.h"
+#include "cs_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Pinned host buffers, reused by size class (powers of two).
+class PinnedPool {
+  public:
+    ~PinnedPool()
+    {
+        for (auto &kv : free_)
+            for (void *p : kv.second) cudaFreeHost(p);
+    }
+    void *get(size_t bytes, size_t *cls)
+    {
+        size_t c = 4096;
+        while (c < bytes) c <<= 1;
+        *cls = c;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto &v = free_[c];
+            if (!v.empty()) {
+                void *p = v.back();
+                v.pop_back();
+                return p;
+            }
+        }
+        void *p = nullptr;
+        if (cudaHostAlloc(&p, c, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+        return p;
+    }
+    void put(void *p, size_t cls)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        free_[cls].push_back(p);
+    }
+
+  private:
+    std::mutex mu_;
+    std::map<size_t, std::vector<void *>> free_;
+};
+
+enum class State { Queued, Active, Draining, Done, Failed };
+// `retired` is set (under the server lock) once the worker holds no more
+// references to a request; only then may a waiter consume and delete it.
+
+struct Request {
+    long long id = 0;
+    cs_plan *plan = nullptr;
+    cs_precision prec = CS_PREC_FP64;
+    cs_layout layout{};
+    long long steps = 0, issued = 0, sweeps_per_step = 1;
+    void *host = nullptr;  // pinned: packed input, later the packed FP64 result
+    size_t host_cls = 0;
+    void *d[2] = {nullptr, nullptr};
+    void *stage = nullptr;  // FP64 staging for split conversions
+    int cur = 0;            // buffer holding the current state
+    size_t bytes = 0;       // device bytes reserved
+    cudaStream_t stream = nullptr;
+    cudaEvent_t chunk_ev = nullptr, done_ev = nullptr;
+    bool chunk_pending = false;
+    cudaGraphExec_t graph = nullptr;
+    long long graph_steps = 0;
+    int full_chunks = 0;
+    double t_submit = 0, t_done = 0;
+    std::atomic<State> state{State::Queued};
+    bool retired = false;
+    cs_status status = CS_OK;
+    std::string error;
+};
+
+}  // namespace
+
+struct cs_server {
+    cs_server_config cfg{};
+    int device = 0;
+    std::vector<cudaStream_t> streams;
+    PinnedPool pinned;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request *> queue;
+    std::vector<Request *> active;
+    std::map<long long, std::unique_ptr<Request>> all;
+    long long next_id = 1;
+    size_t budget = 0, reserved = 0;
+    bool stop = false;
+    std::thread worker;
+    // statistics
+    std::vector<double> latencies;
+    long long completed = 0, failed = 0;
+    double point_steps = 0, t_first = 0, t_last = 0;
+    int rr = 0;
+};
+
+namespace {
+
+void fail_request(cs_server *s, Request *r, cs_status st, const std::string &msg)
+{
+    r->status = st;
+    r->error = msg;
+    r->state = State::Failed;
+    r->t_done = now_s();
+    s->failed++;
+}
+
+// Device buffers come from the stream-ordered pool (cudaMallocAsync), so
+// admitting and retiring requests never synchronises the device.
+void release_device(Request *r)
+{
+    for (void *&p : r->d)
+        if (p) cudaFreeAsync(p, r->stream), p = nullptr;
+    if (r->stage) cudaFreeAsync(r->stage, r->stream), r->stage = nullptr;
+    if (r->graph) cudaGraphExecDestroy(r->graph), r->graph = nullptr;
+    if (r->chunk_ev) cudaEventDestroy(r->chunk_ev), r->chunk_ev = nullptr;
+}
+
+// Allocates and uploads an admitted request (worker thread).
+bool start_request(cs_server *s, Request *r)
+{
+    const size_t b = r->layout.bytes;
+    r->stream = s->streams[s->rr++ % s->streams.size()];
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMallocAsync(&r->d[i], b, r->stream);
+    if (e == cudaSuccess && r->prec == CS_PREC_SPLIT) e = cudaMallocAsync(&r->stage, b, r->stream);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->chunk_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->done_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        fail_request(s, r, e == cudaErrorMemoryAllocation ? CS_ERR_OUT_OF_MEMORY : CS_ERR_CUDA,
+                     cudaGetErrorString(e));
+        return false;
+    }
+    cudaMemsetAsync(r->d[1], 0, b, r->stream);
+    if (r->prec == CS_PREC_FP64) {
+        e = cudaMemcpyAsync(r->d[0], r->host, b, cudaMemcpyHostToDevice, r->stream);
+    } else {
+        e = cudaMemcpyAsync(r->stage, r->host, b, cudaMemcpyHostToDevice, r->stream);
+        if (e == cudaSuccess && cs_split_from_fp64(r->plan, (const double *)r->stage, r->d[0], r->stream) != CS_OK)
+            e = cudaErrorUnknown;
+    }
+    if (e != cudaSuccess) {
+        fail_request(s, r, CS_ERR_CUDA, cudaGetErrorString(e));
+        return false;
+    }
+    r->cur = 0;
+    r->state = State::Active;
+    return true;
+}
+
+// Issues `steps` steps of r on its stream, re-anchoring split grids through
+// FP64 whenever the request's global step count crosses a multiple of 100.
+cs_status issue_steps(Request *r, long long steps)
+{
+    int in_b = 0;
+    cs_status st = cs_run(r->plan, r->d[r->cur], r->d[r->cur ^ 1], steps, r->stream, &in_b);
+    if (st != CS_OK) return st;
+    r->cur ^= in_b;
+    if (r->prec == CS_PREC_SPLIT) {
+        const long long before = r->issued / r->sweeps_per_step / 100;
+        const long long after = (r->issued + steps) / r->sweeps_per_step / 100;
+        if (after != before &&
+            cs::launch_split_reanchor(r->layout.elements, (float2 *)r->d[r->cur], r->stream) != cudaSuccess)
+            return CS_ERR_CUDA;
+    }
+    return CS_OK;
+}
+
+// One scheduling turn for an active request: the next chunk of steps.
+void advance(cs_server *s, Request *r)
+{
+    if (r->chunk_pending) {
+        if (cudaEventQuery(r->chunk_ev) == cudaErrorNotReady) return;  // at most one chunk in flight
+        r->chunk_pending = false;
+    }
+    // Chunks are whole fused sweeps: a multiple of the plan's steps per sweep.
+    const long long full = std::max(1LL, s->cfg.chunk_steps / r->sweeps_per_step) * r->sweeps_per_step;
+    const long long chunk = std::min(full, r->steps - r->issued);
+    cs_status st = CS_OK;
+    const bool graphable = s->cfg.use_graphs && chunk == full &&
+                           (chunk / r->sweeps_per_step) % 2 == 0 && r->prec == CS_PREC_FP64;
+    if (graphable && r->graph && r->graph_steps == chunk) {
+        st = cudaGraphLaunch(r->graph, r->stream) == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+    } else if (graphable && r->full_chunks >= 1) {
+        // Capture one chunk (an even number of sweeps returns to the same
+        // buffer, so the graph can be replayed as is).
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const int cur = r->cur;
+            st = issue_steps(r, chunk);
+            r->cur = cur;
+            e = cudaStreamEndCapture(r->stream, &g);
+        }
+        if (e == cudaSuccess && st == CS_OK && cudaGraphInstantiate(&r->graph, g, 0) == cudaSuccess) {
+            r->graph_steps = chunk;
+            st = cudaGraphLaunch(r->graph, r->stream) == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+        } else if (st == CS_OK) {
+            st = issue_steps(r, chunk);  // capture unavailable: plain launches
+        }
+        if (g) cudaGraphDestroy(g);
+    } else {
+        st = issue_steps(r, chunk);
+    }
+    if (st != CS_OK) {
+        fail_request(s, r, st, cs_last_error());
+        return;
+    }
+    if (chunk == full) r->full_chunks++;
+    r->issued += chunk;
+    if (r->issued >= r->steps) {
+        const void *res = r->d[r->cur];
+        if (r->prec == CS_PREC_SPLIT) {
+            cs_split_to_fp64(r->plan, res, (double *)r->stage, r->stream);
+            res = r->stage;
+        }
+        cudaMemcpyAsync(r->host, res, r->layout.bytes, cudaMemcpyDeviceToHost, r->stream);
+        cudaEventRecord(r->done_ev, r->stream);
+        r->state = State::Draining;
+    } else {
+        cudaEventRecord(r->chunk_ev, r->stream);
+        r->chunk_pending = true;
+    }
+}
+
+void worker_main(cs_server *s)
+{
+    cudaSetDevice(s->device);
+    for (;;) {
+        std::vector<Request *> admitted;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->stop && s->queue.empty() && s->active.empty()) return;
+            if (s->queue.empty() && s->active.empty())
+                s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
+            while (!s->queue.empty() && (int)s->active.size() < s->cfg.max_active) {
+                Request *r = s->queue.front();
+                if (s->reserved + r->bytes > s->budget) {
+                    if (s->active.empty()) {  // can never fit
+                        s->queue.pop_front();
+                        fail_request(s, r, CS_ERR_OUT_OF_MEMORY, "request exceeds the server's HBM budget");
+                        r->retired = true;
+                        s->cv_done.notify_all();
+                        continue;
+                    }
+                    break;  // wait for memory
+                }
+                s->queue.pop_front();
+                s->reserved += r->bytes;
+                s->active.push_back(r);
+                admitted.push_back(r);
+            }
+        }
+        for (Request *r : admitted) {
+            if (!start_request(s, r)) {
+                std::lock_guard<std::mutex> lk(s->mu);
+                release_device(r);
+                s->reserved -= r->bytes;
+                s->active.erase(std::find(s->active.begin(), s->active.end(), r));
+                r->retired = true;
+                s->cv_done.notify_all();
+            }
+        }
+        std::vector<Request *> act;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            act = s->active;
+        }
+        bool progressed = false;
+        for (Request *r : act) {
+            if (r->state == State::Active) {
+                const long long before = r->issued;
+                advance(s, r);
+                progressed |= r->issued != before;
+            }
+            const bool finished = r->state == State::Draining && cudaEventQuery(r->done_ev) == cudaSuccess;
+            if (finished || r->state == State::Failed) {
+                std::lock_guard<std::mutex> lk(s->mu);
+                if (finished) {
+                    r->t_done = now_s();
+                    r->state = State::Done;
+                    s->latencies.push_back(r->t_done - r->t_submit);
+                    s->completed++;
+                    double pts = 1;
+                    for (int d = 0; d < r->layout.dims; ++d) pts *= (double)r->layout.extent[d];
+                    s->point_steps += pts * (double)r->steps;
+                    s->t_last = r->t_done;
+                }
+                release_device(r);
+                s->reserved -= r->bytes;
+                s->active.erase(std::find(s->active.begin(), s->active.end(), r));
+                r->retired = true;
+                s->cv_done.notify_all();
+                progressed = true;
+            }
+        }
+        if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+// Packs a dense interior (row-major) into the plan's layout, zero halo.
+void pack(const cs_layout &L, const double *interior, double *buf)
+{
+    memset(buf, 0, L.bytes);
+    const long long nx = L.extent[L.dims - 1];
+    const long long rows = L.dims == 1 ? 1 : L.dims == 2 ? L.extent[0] : L.extent[0] * L.extent[1];
+    for (long long r = 0; r < rows; ++r) {
+        long long off = L.origin;
+        if (L.dims == 2) off += r * L.pitch[0];
+        if (L.dims == 3) off += (r / L.extent[1]) * L.pitch[0] + (r % L.extent[1]) * L.pitch[1];
+        memcpy(buf + off, interior + r * nx, nx * sizeof(double));
+    }
+}
+
+void unpack(const cs_layout &L, const double *buf, double *interior)
+{
+    const long long nx = L.extent[L.dims - 1];
+    const long long rows = L.dims == 1 ? 1 : L.dims == 2 ? L.extent[0] : L.extent[0] * L.extent[1];
+    for (long long r = 0; r < rows; ++r) {
+        long long off = L.origin;
+        if (L.dims == 2) off += r * L.pitch[0];
+        if (L.dims == 3) off += (r / L.extent[1]) * L.pitch[0] + (r % L.extent[1]) * L.pitch[1];
+        memcpy(interior + r * nx, buf + off, nx * sizeof(double));
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+CS_API cs_status cs_server_create(cs_server **out, const cs_server_config *cfg)
+{
+    if (!out) return CS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cs_server_config c{8, 64, 0.8, 32, 1};
+    if (cfg) c = *cfg;
+    if (c.streams < 1 || c.streams > 128 || c.max_active < 1 || c.hbm_fraction <= 0 || c.hbm_fraction > 1 ||
+        c.chunk_steps < 1)
+        return CS_ERR_INVALID_ARGUMENT;
+    auto s = std::make_unique<cs_server>();
+    s->cfg = c;
+    if (cudaGetDevice(&s->device) != cudaSuccess) return CS_ERR_NO_DEVICE;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return CS_ERR_CUDA;
+    s->budget = (size_t)(c.hbm_fraction * (double)free_b);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
+        unsigned long long keep = s->budget;  // keep freed blocks for the next admissions
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    for (int i = 0; i < c.streams; ++i) {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CS_ERR_CUDA;
+        s->streams.push_back(st);
+    }
+    s->worker = std::thread(worker_main, s.get());
+    *out = s.release();
+    return CS_OK;
+}
+
+CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long long *id)
+{
+    if (!s || !d || !id || !d->interior_in || !d->weights || d->steps < 0) return CS_ERR_INVALID_ARGUMENT;
+    auto r = std::make_unique<Request>();
+    cs_status st = cs_plan_create(&r->plan, d->shape, d->semantics, d->precision, d->extent, d->weights,
+                                  d->n_weights, nullptr);
+    if (st != CS_OK) return st;
+    // A fixed kernel choice (no timing-dependent tuning) keeps results
+    // identical in any mix: the FP64 FMA kernels, and for split precision
+    // the tensor-core slice kernel where it applies.
+    if (d->precision == CS_PREC_SPLIT) {
+        if (cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_SPLIT_MMA) != CS_OK)
+            cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_SPLIT_FMA);
+    } else {
+        cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_FMA);
+    }
+    cs_plan_set_option(r->plan, CS_OPT_REANCHOR_INTERVAL, 0);  // the server re-anchors at global steps
+    long long sweeps1 = 0;
+    if (d->semantics == CS_SEM_FUSED) {
+        for (long long k = 1; k <= 3; ++k)
+            if (cs_plan_sweeps(r->plan, k, &sweeps1) == CS_OK && sweeps1 == 1) {
+                r->sweeps_per_step = k;
+                break;
+            }
+    }
+    if (cs_plan_sweeps(r->plan, d->steps, &sweeps1) != CS_OK) {
+        cs_plan_destroy(r->plan);
+        return CS_ERR_INVALID_ARGUMENT;
+    }
+    cs_plan_get_layout(r->plan, &r->layout);
+    r->prec = d->precision;
+    r->steps = d->steps;
+    r->bytes = r->layout.bytes * (d->precision == CS_PREC_SPLIT ? 3 : 2);
+    r->host = s->pinned.get(r->layout.bytes, &r->host_cls);
+    if (!r->host) {
+        cs_plan_destroy(r->plan);
+        return CS_ERR_OUT_OF_MEMORY;
+    }
+    pack(r->layout, d->interior_in, (double *)r->host);
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->id = s->next_id++;
+    r->t_submit = now_s();
+    if (s->t_first == 0) s->t_first = r->t_submit;
+    *id = r->id;
+    Request *raw = r.get();
+    s->all[r->id] = std::move(r);
+    if (raw->steps == 0) {  // nothing to run: the result is the input
+        raw->state = State::Done;
+        raw->retired = true;
+        raw->t_done = raw->t_submit;
+        s->completed++;
+        s->latencies.push_back(0.0);
+        s->cv_done.notify_all();
+    } else {
+        s->queue.push_back(raw);
+        s->cv_work.notify_one();
+    }
+    return CS_OK;
+}
+
+CS_API cs_status cs_server_wait(cs_server *s, long long id, double *interior_out, double timeout_seconds,
+                                double *latency_seconds)
+{
+    if (!s) return CS_ERR_INVALID_ARGUMENT;
+    Request *r = nullptr;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return CS_ERR_INVALID_ARGUMENT;
+    r = it->second.get();
+    const auto deadline = std::chrono::steady_clock::now() +
+                          std::chrono::duration<double>(timeout_seconds > 0 ? timeout_seconds : 1e9);
+    while (!r->retired) {
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !r->retired)
+            return CS_ERR_TIMEOUT;
+    }
+    cs_status st = r->status;
+    if (r->state == State::Done && interior_out) unpack(r->layout, (const double *)r->host, interior_out);
+    if (latency_seconds) *latency_seconds = r->t_done - r->t_submit;
+    if (r->done_ev) cudaEventDestroy(r->done_ev);
+    s->pinned.put(r->host, r->host_cls);
+    cs_plan_destroy(r->plan);
+    s->all.erase(it);
+    return st;
+}
+
+CS_API cs_status cs_server_get_stats(cs_server *s, cs_server_stats *out)
+{
+    if (!s || !out) return CS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    memset(out, 0, sizeof *out);
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->queued = (long long)s->queue.size();
+    out->active = (long long)s->active.size();
+    out->hbm_budget_bytes = (long long)s->budget;
+    out->hbm_reserved_bytes = (long long)s->reserved;
+    std::vector<double> v = s->latencies;
+    if (!v.empty()) {
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))]; };
+        out->p50_s = pct(0.50);
+        out->p99_s = pct(0.99);
+        double sum = 0;
+        for (double x : v) sum += x;
+        out->mean_s = sum / (double)v.size();
+    }
+    out->point_steps = s->point_steps;
+    out->wall_s = s->t_last > s->t_first ? s->t_last - s->t_first : 0.0;
+    out->gstencil_s = out->wall_s > 0 ? s->point_steps / out->wall_s / 1e9 : 0.0;
+    return CS_OK;
+}
+
+CS_API cs_status cs_server_destroy(cs_server *s)
+{
+    if (!s) return CS_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    for (auto &kv : s->all) {
+        Request *r = kv.second.get();
+        release_device(r);
+        if (r->done_ev) cudaEventDestroy(r->done_ev);
+        if (r->host) s->pinned.put(r->host, r->host_cls);
+        cs_plan_destroy(r->plan);
+    }
+    for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
+    delete s;
+    return CS_OK;
+}
+
+}  // extern "C"

@@ -188,6 +188,55 @@ CS_API cs_status cs_gpu_box_3d1r(const double *in, double *out, const double *pa
 CS_API cs_status cs_gpu_star_3d1r(const double *in, double *out, const double *params,
                                   int times, int input_h, int input_m, int input_n);
 
+/* ---- serving: continuous batching of stencil solves --------------------- */
+/* A worker thread admits requests while their device buffers fit in the HBM
+ * budget and a slot is free, keeps their grids device-resident, and issues
+ * one chunk of sweeps per active request per turn on a pool of streams (the
+ * work of different requests overlaps on the GPU; full chunks are replayed as
+ * captured CUDA graphs). Kernel choice and re-anchoring depend only on the
+ * request, so a result is bitwise the same alone and in any mix. Not in the
+ * reference (its CLIs run one solve per process). */
+typedef struct cs_server cs_server;
+typedef struct cs_server_config {
+    int streams;           /* CUDA streams shared by the active requests (default 8) */
+    int max_active;        /* requests resident on the GPU at once (default 64) */
+    double hbm_fraction;   /* share of the device memory free at creation the server may use (0.8) */
+    long long chunk_steps; /* steps issued per request per scheduling turn (default 32) */
+    int use_graphs;        /* replay full FP64 chunks as captured CUDA graphs (default 1) */
+} cs_server_config;
+typedef struct cs_request_desc {
+    cs_shape shape;
+    cs_semantics semantics;
+    cs_precision precision;
+    long long extent[3];       /* interior sizes, slowest first */
+    const double *weights;
+    int n_weights;
+    const double *interior_in; /* dense row-major interior, FP64 (halo is zero) */
+    long long steps;
+} cs_request_desc;
+typedef struct cs_server_stats {
+    long long completed, failed, queued, active;
+    long long hbm_budget_bytes, hbm_reserved_bytes;
+    double p50_s, p99_s, mean_s; /* submit -> result on the host */
+    double point_steps;          /* interior points x steps of completed requests */
+    double wall_s;               /* first submit -> last completion */
+    double gstencil_s;           /* point_steps / wall_s / 1e9 */
+} cs_server_stats;
+
+/* cfg NULL = defaults. Uses the calling thread's current device. */
+CS_API cs_status cs_server_create(cs_server **server, const cs_server_config *cfg);
+/* Copies the input; returns at once with the request id. */
+CS_API cs_status cs_server_submit(cs_server *server, const cs_request_desc *req, long long *id);
+/* Waits (timeout_seconds <= 0: no limit) and copies the dense interior result
+ * to interior_out (may be NULL). Returns the request's status (e.g.
+ * CS_ERR_OUT_OF_MEMORY if it can never fit the budget), CS_ERR_TIMEOUT if not
+ * finished in time. Each id is waited for once. */
+CS_API cs_status cs_server_wait(cs_server *server, long long id, double *interior_out,
+                                double timeout_seconds, double *latency_seconds);
+CS_API cs_status cs_server_get_stats(cs_server *server, cs_server_stats *out);
+/* Finishes the admitted and queued work, then releases everything. */
+CS_API cs_status cs_server_destroy(cs_server *server);
+
 /* ---- utilities --------------------------------------------------------- */
 CS_API const char *cs_status_string(cs_status s);
 CS_API const char *cs_last_error(void);
