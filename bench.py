@@ -181,6 +181,17 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------ pipe peaks
+def run_pipe_peaks():
+    """FP64 / FP32 / tensor pipe issue rates (convstencil_gb300/csrc/peaks/pipe_peaks.cu)."""
+    from convstencil_gb300 import build_lib
+    src = os.path.join(ROOT, "convstencil_gb300", "csrc", "peaks", "pipe_peaks.cu")
+    exe = os.path.join(ROOT, "convstencil_gb300", "_lib", "pipe_peaks")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    subprocess.check_call([build_lib.nvcc()] + build_lib.ARCH + ["-O3", "-o", exe, src])
+    return subprocess.call([exe])
+
+
 # ------------------------------------------------------------ ncu cases
 def run_kernel_case(args):
     """One box2d3r plan, one algorithm, `sweeps` sweeps on an m x n grid."""
@@ -191,7 +202,8 @@ def run_kernel_case(args):
     x = O.splitmix_uniform(m * n, GRID_SEED).reshape(m, n)
     w = O.seeded_weights(TAPS, WEIGHT_SEED)
     algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA,
-            "split_mma": cs.Algo.SPLIT_MMA, "split_fma": cs.Algo.SPLIT_FMA}[args.kernel_case]
+            "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
+            "split_fma": cs.Algo.SPLIT_FMA}[args.kernel_case]
     split = args.kernel_case.startswith("split")
     p = cs.Plan(SHAPE, (m, n), w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
     p.set_option(cs.Option.ALGO, algo)
@@ -214,6 +226,62 @@ def run_kernel_case(args):
     return 0
 
 
+# ------------------------------------------------------------ served stream
+def served_stream(n_requests, rate_hz, seed, dev_index):
+    """BASELINE config 5 as a bounded sample: n_requests with Poisson arrivals
+    (rate_hz), shape uniform over {star2d1r, box2d3r, star3d1r, box3d1r}, 2D
+    sides log-uniform 64..4096, 3D sides log-uniform 32..256, steps uniform
+    10..500, half FP64 and half split precision, seeded weights normalised to
+    sum 1 and grids uniform [0,1). Returns the server's latency statistics."""
+    import threading
+    import convstencil_gb300 as cs
+    from oracle import cs_oracle as O
+    rng = np.random.default_rng(seed)
+    shapes = ["star2d1r", "box2d3r", "star3d1r", "box3d1r"]
+    reqs = []
+    for i in range(n_requests):
+        shape = shapes[int(rng.integers(0, 4))]
+        info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
+        if info[0] == 2:
+            ext = tuple(int(v) for v in np.exp(rng.uniform(np.log(64), np.log(4096), 2)))
+        else:
+            ext = tuple(int(v) for v in np.exp(rng.uniform(np.log(32), np.log(256), 3)))
+        steps = int(rng.integers(10, 501))
+        prec = cs.Precision.SPLIT if rng.random() < 0.5 else cs.Precision.FP64
+        w = O.seeded_weights(info[1], 1000 + i)
+        x = np.random.default_rng(seed * 7919 + i).random(ext)
+        reqs.append((shape, x, w, steps, prec))
+    gaps = rng.exponential(1.0 / rate_hz, n_requests)
+    srv = cs.Server(streams=8, max_active=32, hbm_fraction=0.5, chunk_steps=32)
+    ids = [None] * n_requests
+    lat = [None] * n_requests
+
+    def waiter():
+        for i in range(n_requests):
+            while ids[i] is None:
+                time.sleep(1e-4)
+            lat[i] = srv.wait(ids[i], timeout=600)[1]
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    t_next = t0
+    for i, (shape, x, w, steps, prec) in enumerate(reqs):
+        t_next += gaps[i]
+        d = t_next - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ids[i] = srv.submit(shape, x, w, steps, precision=prec)
+    th.join()
+    st = srv.stats()
+    srv.close()
+    return {"requests": n_requests, "arrival_rate_hz": rate_hz,
+            "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
+            "mean_ms": round(st["mean_s"] * 1e3, 3), "gstencil_s": round(st["gstencil_s"], 3),
+            "completed": st["completed"], "failed": st["failed"],
+            "mix": "star2d1r/box2d3r/star3d1r/box3d1r, 2D 64-4096, 3D 32-256, steps 10-500, 50% split"}
+
+
 # ---------------------------------------------------------------------- ours
 def main():
     ap = argparse.ArgumentParser()
@@ -224,14 +292,21 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--served", type=int, default=96,
+                    help="requests in the served-stream sample (0 = skip)")
+    ap.add_argument("--served-rate", type=float, default=40.0, help="Poisson arrival rate (req/s)")
     ap.add_argument("--kernel-case", default=None,
-                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_fma"],
+                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_mma_tma", "split_fma"],
                     help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid "
                          "(small cases for ncu captures) and exit")
     ap.add_argument("--m", type=int, default=4608)
     ap.add_argument("--n", type=int, default=4608)
     ap.add_argument("--sweeps", type=int, default=4)
+    ap.add_argument("--pipe-peaks", action="store_true",
+                    help="build and run the arithmetic-pipe microbenchmark and exit")
     args = ap.parse_args()
+    if args.pipe_peaks:
+        return run_pipe_peaks()
     if args.impl == "reference":
         return run_reference(args)
     if args.kernel_case:
@@ -241,28 +316,24 @@ def main():
     import torch
     import convstencil_gb300 as cs
 
-    rank, world, local = env_rank()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from convstencil_gb300 import replicas
+    rank, world, local = replicas.world()
     torch.cuda.set_device(local)
+    replicas.init("nccl")
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
+    # Every torch op below (copies, clones, zero fills) runs on the same stream
+    # as the library's launches, so all of them are ordered.
+    torch.cuda.set_stream(stream)
 
     x, w = seeded_inputs()
     peaks, peak_src = load_peaks()
     K, W = args.steps, args.warmup
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    barrier = replicas.barrier
 
     def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.reduce_max(v, dev)
 
     def timed_device_run(plan, a, b, steps, sampler=None):
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -363,7 +434,8 @@ def main():
         pk = float(peaks["hbm_gbs"])
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": pk, "unit": "GB/s",
                 "frac": round(ach / pk, 4), "traffic": profile_traffic("split_box2d3r_sweep"),
-                "kernel": "split sweep", "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": f"split sweep ({psp.algo.name})",
+                "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic": f"16 B/pt (8 B read + 8 B write) x {M}x{N} pts per launch"}
 
     # ---------------- e2e through the reference-shaped C ABI (host buffers)
@@ -412,6 +484,10 @@ def main():
         cpu = {"value": round(work / t / 1e9, 4), "unit": "GStencil/s", "cores": cores, "kind": "port",
                "sample": f"1 sweep of a {rows}x{N} slab of the same grid (OpenMP C oracle)"}
 
+    served = None
+    if args.served > 0:
+        served = served_stream(args.served, args.served_rate, 17 + rank, local)
+
     if rank != 0:
         return 0
     clocks = hr["clocks"]
@@ -419,12 +495,12 @@ def main():
         "metric": METRIC, "value": round(value, 4), "unit": "GStencil/s", "n_gpus": world,
         "steps": K, "warmup": W, "ms_per_step": round(hr["seconds"] / K * 1e3, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32x2 split (bf16 slices, f32 accum)" if headline == "split" else "f64",
+        "dtype": "f32x2 split (exact fp16 slices, f32 accum)" if headline == "split" else "f64",
         "data": "synthetic (SplitMix64 seeded grid and weights)",
         "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": K, "precision": headline,
                    "l2": "inputs larger than L2 (537 MB per grid vs 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
-        "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
+        "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "served": served,
         "gpu_launches": hr["launches"], "clocks": clocks,
     }
     if "fp64" in results:

@@ -148,6 +148,7 @@ def lib() -> ctypes.CDLL:
     L.cs_plan_get_layout.argtypes = [vp, ctypes.POINTER(Layout)]
     L.cs_plan_sweeps.argtypes = [vp, ll, ctypes.POINTER(ll)]
     L.cs_plan_destroy.argtypes = [vp]
+    L.cs_plan_get_algo.argtypes = [vp, ctypes.POINTER(i)]
     L.cs_run.argtypes = [vp, vp, vp, ll, vp, ctypes.POINTER(i)]
     L.cs_run_host.argtypes = [vp, dp, dp, ll]
     L.cs_split_from_fp64.argtypes = [vp, vp, vp, vp]
@@ -262,6 +263,13 @@ class Plan:
     def set_option(self, opt: Option, value: int) -> "Plan":
         check(lib().cs_plan_set_option(self._h, int(opt), int(value)))
         return self
+
+    @property
+    def algo(self) -> "Algo":
+        """Kernel family of the last run (the tuner's pick under AUTO)."""
+        a = ctypes.c_int()
+        check(lib().cs_plan_get_algo(self._h, ctypes.byref(a)))
+        return Algo(a.value)
 
     def sweeps(self, steps: int) -> int:
         s = ctypes.c_longlong()

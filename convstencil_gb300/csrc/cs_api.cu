@@ -217,6 +217,7 @@ struct cs_plan {
     cs_layout layout;
     GridView view;
     int algo = CS_ALGO_AUTO;
+    int last_algo = CS_ALGO_AUTO;  // kernel family the last cs_run used
     long long reanchor = 100;
 };
 
@@ -476,6 +477,13 @@ CS_API cs_status cs_plan_sweeps(const cs_plan *p, long long steps, long long *sw
     return CS_OK;
 }
 
+CS_API cs_status cs_plan_get_algo(const cs_plan *p, int *algo)
+{
+    if (!p || !algo) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    *algo = p->last_algo;
+    return CS_OK;
+}
+
 CS_API cs_status cs_plan_destroy(cs_plan *p)
 {
     delete p;
@@ -494,6 +502,7 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
     if (sweeps > 0) {
         s = choose_algo(p, a, b, st, &algo);
         if (s != CS_OK) return s;
+        p->last_algo = algo;
     }
     void *buf[2] = {a, b};
     for (long long i = 0; i < sweeps; ++i) {

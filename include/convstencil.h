@@ -123,6 +123,9 @@ CS_API cs_status cs_plan_get_layout(const cs_plan *plan, cs_layout *out);
 /* Sweep count and steps per sweep for `steps` steps (FUSED: steps must be a
  * multiple of the fused step count). */
 CS_API cs_status cs_plan_sweeps(const cs_plan *plan, long long steps, long long *sweeps);
+/* The cs_algo the plan's last cs_run used (its tuner's choice under
+ * CS_ALGO_AUTO); CS_ALGO_AUTO before the first run. */
+CS_API cs_status cs_plan_get_algo(const cs_plan *plan, int *algo);
 CS_API cs_status cs_plan_destroy(cs_plan *plan);
 
 /* Runs `steps` steps from buffer a, ping-ponging with b (both per the plan's
