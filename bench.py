@@ -181,6 +181,28 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------ reference GPU kernel
+def run_reference_gpu(args):
+    """Reported baseline: the reference's own kernel2d (compiled from its
+    sources for sm_103a, oracle/_ref/ref_2d.cubin) on the same workload,
+    launched as its wrapper does; CUDA-event time of the launch loop."""
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        print(json.dumps({"impl": "reference-gpu", "unavailable": "reference cubins not built"}))
+        return 0
+    x, w = seeded_inputs()
+    g = np.zeros((M + 6, N + 8))
+    g[3:M + 3, 4:N + 4] = x
+    ref_gpu.box_2d(g, w, max(1, args.warmup), M, N)
+    _, secs = ref_gpu.box_2d(g, w, args.steps, M, N)
+    val = float(M) * N * args.steps / secs / 1e9
+    print(json.dumps({"impl": "reference-gpu", "metric": METRIC, "value": round(val, 4),
+                      "unit": "GStencil/s", "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
+                      "dtype": "f64", "kernel": "reference kernel2d (DMMA m8n8k4, dual tessellation)",
+                      "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": args.steps}}), flush=True)
+    return 0
+
+
 # ------------------------------------------------------------ pipe peaks
 def run_pipe_peaks():
     """FP64 / FP32 / tensor pipe issue rates (convstencil_gb300/csrc/peaks/pipe_peaks.cu)."""
@@ -288,7 +310,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-gpu"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -309,6 +331,8 @@ def main():
         return run_pipe_peaks()
     if args.impl == "reference":
         return run_reference(args)
+    if args.impl == "reference-gpu":
+        return run_reference_gpu(args)
     if args.kernel_case:
         return run_kernel_case(args)
     args.warmup = max(3, args.warmup)

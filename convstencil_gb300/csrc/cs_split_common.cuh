@@ -44,18 +44,20 @@ __device__ __forceinline__ unsigned pack_h2(float lo_elem, float hi_elem)
     return *reinterpret_cast<const unsigned *>(&h);
 }
 
-// Cuts x' = (a + b) (|x'| < 256 after the first scaling) into five balanced
-// base-512 digits. Every step is exact: rint(a) is an integer within 1/2 of
-// a, a - rint(a) is representable, and two_sum keeps (a, b) normalised.
+// Cuts x' = a + b (|a| < 256, |b| <= ulp(a)/2 after the power-of-two scaling)
+// into five balanced base-512 digits. The remainder after each digit is kept
+// exactly as the unevaluated pair (a - d, b): a - d is exact (both are
+// multiples of a's last bit g, and |a - d| < 1 or both are integers), b stays
+// below g/2, and scaling by 512 is exact, so no renormalisation is needed.
+// d = rint(a + b) may differ from the exact rounding by one ulp of the sum;
+// the next remainder then stays within 1/2 + 2^-24 and every digit within 256.
 __device__ __forceinline__ void slice_digits(float a, float b, float (&d)[kDigits])
 {
 #pragma unroll
     for (int k = 0; k < kDigits - 1; ++k) {
-        d[k] = rintf(a);
-        float s, e;
-        two_sum(a - d[k], b, s, e);
-        a = s * kRadix;
-        b = e * kRadix;
+        d[k] = rintf(a + b);
+        a = (a - d[k]) * kRadix;
+        b = b * kRadix;
     }
     d[kDigits - 1] = rintf(a + b);
 }

@@ -23,5 +23,13 @@ nvcc $ARCH $COMMON -Dmain=cs_ref_main_2d -I"$REF/src/2d" \
 nvcc $ARCH $COMMON -Dmain=cs_ref_main_3d -I"$REF/src/3d" \
     "$HERE/ref_harness/ref_naive_3d.cu" "$REF/src/3d/gpu_box.cu" "$REF/src/3d/gpu_star.cu" \
     -o "$OUT/libref_naive_3d.so" &
+# The reference's GPU kernels as sm_103a cubins, for the reference-GPU baseline
+# and GPU-to-GPU parity (loaded with the driver API by oracle/ref_gpu.py).
+CUBIN="-cubin -O3 -w $ARCH"
+nvcc $CUBIN -I"$REF/src/2d" "$REF/src/2d/gpu.cu" -o "$OUT/ref_2d.cubin" &
+nvcc $CUBIN -I"$REF/src/1d" "$HERE/ref_harness/ref_cubin_1d1r.cu" -o "$OUT/ref_1d1r.cubin" &
+nvcc $CUBIN -I"$REF/src/1d" "$HERE/ref_harness/ref_cubin_1d2r.cu" -o "$OUT/ref_1d2r.cubin" &
+nvcc $CUBIN -I"$REF/src/3d" "$REF/src/3d/gpu_box.cu" -o "$OUT/ref_3d_box.cubin" &
+nvcc $CUBIN -I"$REF/src/3d" "$REF/src/3d/gpu_star.cu" -o "$OUT/ref_3d_star.cubin" &
 wait
-echo "built reference CPU stencils into $OUT"
+echo "built reference CPU stencils and GPU cubins into $OUT"
