@@ -82,6 +82,7 @@ class Algo(enum.IntEnum):
 class Option(enum.IntEnum):
     ALGO = 0
     REANCHOR_INTERVAL = 2
+    TIME_BLOCK = 3
 
 
 class Layout(ctypes.Structure):
@@ -149,6 +150,7 @@ def lib() -> ctypes.CDLL:
     L.cs_plan_sweeps.argtypes = [vp, ll, ctypes.POINTER(ll)]
     L.cs_plan_destroy.argtypes = [vp]
     L.cs_plan_get_algo.argtypes = [vp, ctypes.POINTER(i)]
+    L.cs_plan_get_time_block.argtypes = [vp, ctypes.POINTER(i)]
     L.cs_run.argtypes = [vp, vp, vp, ll, vp, ctypes.POINTER(i)]
     L.cs_run_host.argtypes = [vp, dp, dp, ll]
     L.cs_split_from_fp64.argtypes = [vp, vp, vp, vp]
@@ -270,6 +272,13 @@ class Plan:
         a = ctypes.c_int()
         check(lib().cs_plan_get_algo(self._h, ctypes.byref(a)))
         return Algo(a.value)
+
+    @property
+    def time_block(self) -> int:
+        """Steps per launch of the last run (temporal blocking; 1 = off)."""
+        t = ctypes.c_int()
+        check(lib().cs_plan_get_time_block(self._h, ctypes.byref(t)))
+        return int(t.value)
 
     def sweeps(self, steps: int) -> int:
         s = ctypes.c_longlong()

@@ -11,6 +11,7 @@
 #include "../../include/convstencil.h"
 #include "cs_internal.h"
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -204,7 +205,8 @@ void native_layout(int dims, int r, const long long *ext, cs_layout &L)
 // The tuner's memory: which algorithm won for a (dims, radius, pattern,
 // precision, log2 size) class. Process-wide, guarded by a mutex.
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int, int, int>, int> g_tune;
+std::map<std::tuple<int, int, int, int, int>, int> g_tune;      // -> algorithm
+std::map<std::tuple<int, int, int, int, int>, int> g_tune_tb;   // -> steps per launch (split FMA)
 
 }  // namespace
 
@@ -218,6 +220,8 @@ struct cs_plan {
     GridView view;
     int algo = CS_ALGO_AUTO;
     int last_algo = CS_ALGO_AUTO;  // kernel family the last cs_run used
+    int time_block = 0;            // split FMA: steps per launch (0 = tuner)
+    int last_time_block = 1;
     long long reanchor = 100;
 };
 
@@ -338,6 +342,63 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
     return CS_OK;
 }
 
+// Steps per launch for the double-float split kernels (temporal blocking).
+// With time_block 0 the first run times T = 1..4 once (one launch each on
+// a -> b; every candidate computes the same sweeps) and remembers the fastest
+// per step for plans of the same class.
+cs_status choose_time_block(cs_plan *p, int algo, const void *a, void *b, cudaStream_t st, int *out)
+{
+    *out = 1;
+    if (p->prec != CS_PREC_SPLIT || algo != CS_ALGO_SPLIT_FMA ||
+        !cs::split_tb_supported(p->dims, p->radius, p->pattern))
+        return CS_OK;
+    if (p->time_block > 0) {
+        *out = p->time_block;
+        return CS_OK;
+    }
+    auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_tb.find(key);
+        if (it != g_tune_tb.end()) {
+            *out = it->second;
+            return CS_OK;
+        }
+    }
+    const long long off = p->layout.origin;
+    const float2 *in = (const float2 *)a + off;
+    float2 *o = (float2 *)b + off;
+    cudaEvent_t e0, e1;
+    CS_CUDA(cudaEventCreate(&e0));
+    CS_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_t = 1;
+    for (int rep = 0; rep < 2; ++rep) {
+        for (int t = 1; t <= 4; ++t) {
+            CS_CUDA(cudaEventRecord(e0, st));
+            cudaError_t e = t == 1 ? cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, 0, in, o, st)
+                                   : cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w, in, o, st);
+            if (e != cudaSuccess) return cuda_fail(e, "time-block tuning launch");
+            CS_CUDA(cudaEventRecord(e1, st));
+            CS_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep == 1 && ms / t < best) {
+                best = ms / t;
+                best_t = t;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_tb[key] = best_t;
+    }
+    *out = best_t;
+    return CS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -455,6 +516,12 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
         if (v < 0) return fail(CS_ERR_INVALID_ARGUMENT, "negative re-anchor interval");
         p->reanchor = v;
         return CS_OK;
+    case CS_OPT_TIME_BLOCK:
+        if (v < 0 || v > 4) return fail(CS_ERR_INVALID_ARGUMENT, "time block must be 0 (tuner) or 1..4");
+        if (v > 1 && !(p->prec == CS_PREC_SPLIT && cs::split_tb_supported(p->dims, p->radius, p->pattern)))
+            return fail(CS_ERR_UNSUPPORTED, "temporal blocking serves split-precision 2D radius-1 and 1D plans");
+        p->time_block = (int)v;
+        return CS_OK;
     }
     return fail(CS_ERR_INVALID_ARGUMENT, "unknown option %d", (int)opt);
 }
@@ -484,6 +551,13 @@ CS_API cs_status cs_plan_get_algo(const cs_plan *p, int *algo)
     return CS_OK;
 }
 
+CS_API cs_status cs_plan_get_time_block(const cs_plan *p, int *steps_per_launch)
+{
+    if (!p || !steps_per_launch) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    *steps_per_launch = p->last_time_block;
+    return CS_OK;
+}
+
 CS_API cs_status cs_plan_destroy(cs_plan *p)
 {
     delete p;
@@ -498,22 +572,36 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
     cs_status s = cs_plan_sweeps(p, steps, &sweeps);
     if (s != CS_OK) return s;
     cudaStream_t st = (cudaStream_t)stream;
-    int algo = CS_ALGO_FP64_FMA;
+    int algo = CS_ALGO_FP64_FMA, tb = 1;
     if (sweeps > 0) {
         s = choose_algo(p, a, b, st, &algo);
         if (s != CS_OK) return s;
+        s = choose_time_block(p, algo, a, b, st, &tb);
+        if (s != CS_OK) return s;
         p->last_algo = algo;
+        p->last_time_block = tb;
     }
     void *buf[2] = {a, b};
-    for (long long i = 0; i < sweeps; ++i) {
-        cudaError_t e = launch_sweep(p, algo, buf[i & 1], buf[(i + 1) & 1], st);
+    int cur = 0;
+    const long long off = p->layout.origin;
+    for (long long i = 0; i < sweeps;) {
+        const int t = (int)std::min<long long>(tb, sweeps - i);
+        cudaError_t e;
+        if (t >= 2)
+            e = cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w,
+                                          (const float2 *)buf[cur] + off, (float2 *)buf[cur ^ 1] + off, st);
+        else
+            e = launch_sweep(p, algo, buf[cur], buf[cur ^ 1], st);
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
-        if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && ((i + 1) % p->reanchor) == 0) {
-            e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[(i + 1) & 1], st);
+        cur ^= 1;
+        const long long done = i + t;
+        if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && done / p->reanchor != i / p->reanchor) {
+            e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[cur], st);
             if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
         }
+        i = done;
     }
-    if (result_in_b) *result_in_b = (int)(sweeps & 1);
+    if (result_in_b) *result_in_b = cur;
     return CS_OK;
 }
 

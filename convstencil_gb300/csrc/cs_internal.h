@@ -47,6 +47,11 @@ bool fp64_fma_supported(int dims, int radius, int pattern);
 cudaError_t launch_split_sweep(const GridView &g, int radius, int pattern, const Weights &w,
                                int use_mma, const float2 *in, float2 *out, cudaStream_t stream);
 bool split_supported(int dims, int radius, int pattern);
+// Temporal blocking: T (2..4) steps per launch of the double-float kernels,
+// 2D radius 1 and 1D radius 1-2; bitwise identical to T single sweeps.
+bool split_tb_supported(int dims, int radius, int pattern);
+cudaError_t launch_split_sweep_tb(const GridView &g, int radius, int pattern, int T, const Weights &w,
+                                  const float2 *in, float2 *out, cudaStream_t stream);
 bool split_mma_layout_ok(const GridView &g, long long origin);
 // Warp-specialised TMA variant of the slice kernel (cs_kernels_split_tma.cu);
 // needs an even row pitch, >= 4 halo columns left of the interior (the TMA box

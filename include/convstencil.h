@@ -89,8 +89,11 @@ typedef enum cs_algo {
 
 typedef enum cs_option {
     CS_OPT_ALGO = 0,              /* cs_algo */
-    CS_OPT_REANCHOR_INTERVAL = 2  /* split: renormalise (hi,lo) through FP64 every N
+    CS_OPT_REANCHOR_INTERVAL = 2, /* split: renormalise (hi,lo) through FP64 every N
                                      sweeps (default 100, 0 = never) */
+    CS_OPT_TIME_BLOCK = 3         /* split double-float kernels, 2D radius 1 and 1D:
+                                     steps fused per launch by temporal blocking
+                                     (0 = tuner picks 1..4, default; 1 = off) */
 } cs_option;
 
 /* Where a grid lives in a buffer. extent/pitch are slowest axis first; the
@@ -126,6 +129,8 @@ CS_API cs_status cs_plan_sweeps(const cs_plan *plan, long long steps, long long 
 /* The cs_algo the plan's last cs_run used (its tuner's choice under
  * CS_ALGO_AUTO); CS_ALGO_AUTO before the first run. */
 CS_API cs_status cs_plan_get_algo(const cs_plan *plan, int *algo);
+/* Steps per launch the plan's last cs_run used (temporal blocking; 1 = off). */
+CS_API cs_status cs_plan_get_time_block(const cs_plan *plan, int *steps_per_launch);
 CS_API cs_status cs_plan_destroy(cs_plan *plan);
 
 /* Runs `steps` steps from buffer a, ping-ponging with b (both per the plan's

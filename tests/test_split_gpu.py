@@ -145,3 +145,34 @@ def test_split_roundtrip_conversion():
 def test_no_device_wait_timed_out():
     """The pipelined kernel's bounded waits never expired during this module."""
     assert cs.device_wait_timeouts(reset=True) == 0
+
+
+TB_CASES = [("star2d1r", (97, 150), 7), ("box2d1r", (64, 130), 9), ("1d1r", (5000,), 11),
+            ("1d2r", (3001,), 6)]
+
+
+@pytest.mark.parametrize("shape,ext,steps", TB_CASES)
+def test_temporal_blocking_is_bitwise_equal_and_accurate(shape, ext, steps):
+    info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
+    w = O.seeded_weights(info[1], 700 + info[1])
+    x = O.splitmix_uniform(int(np.prod(ext)), 93).reshape(ext)
+    outs = {}
+    for tb in (1, 2, 3, 4):
+        p = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT)
+        p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_FMA)
+        p.set_option(cs.Option.TIME_BLOCK, tb)
+        outs[tb] = split_run(p, p.pack(x), steps)
+        assert p.time_block == tb
+    for tb in (2, 3, 4):
+        np.testing.assert_array_equal(outs[tb], outs[1])
+    ref = oracle_run(p, p.pack(x), _dense(shape, w), info[4], steps)
+    assert rel_err(p.unpack(outs[4]), p.unpack(ref))[0] <= TOL
+
+
+def test_time_block_option_validation():
+    p = cs.Plan("box2d3r", (64, 64), O.seeded_weights(49, 1), precision=cs.Precision.SPLIT)
+    with pytest.raises(cs.ConvStencilError):
+        p.set_option(cs.Option.TIME_BLOCK, 2)   # radius 3: no temporal blocking
+    q = cs.Plan("star2d1r", (64, 64), O.seeded_weights(5, 1))
+    with pytest.raises(cs.ConvStencilError):
+        q.set_option(cs.Option.TIME_BLOCK, 2)   # FP64 plans are FP64-pipe bound: not offered
