@@ -203,6 +203,35 @@ def run_reference_gpu(args):
     return 0
 
 
+# ------------------------------------------------- library FP64 convolution
+def run_torch_conv(args):
+    """Reported baseline: a library FP64 convolution (torch.nn.functional.conv2d,
+    cuDNN or PyTorch's own kernel) doing the same sweep: 7x7 correlation with
+    zero padding 3 on the 8192^2 grid, ping-pong, CUDA-event time."""
+    import torch
+    import torch.nn.functional as F
+    x, w = seeded_inputs()
+    a = torch.from_numpy(x).cuda().view(1, 1, M, N)
+    k = torch.from_numpy(w.reshape(1, 1, 7, 7)).cuda()
+    for _ in range(max(1, args.warmup)):
+        a = F.conv2d(a, k, padding=3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        a = F.conv2d(a, k, padding=3)
+    e1.record()
+    e1.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3
+    val = float(M) * N * args.steps / secs / 1e9
+    print(json.dumps({"impl": "torch-conv", "metric": METRIC, "value": round(val, 4), "unit": "GStencil/s",
+                      "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4), "dtype": "f64",
+                      "kernel": "torch.nn.functional.conv2d float64 (cudnn enabled: %s)"
+                                % torch.backends.cudnn.is_available(),
+                      "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": args.steps}}), flush=True)
+    return 0
+
+
 # ------------------------------------------------------------ pipe peaks
 def run_pipe_peaks():
     """FP64 / FP32 / tensor pipe issue rates (convstencil_gb300/csrc/peaks/pipe_peaks.cu)."""
@@ -310,7 +339,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-gpu"])
+    ap.add_argument("--impl", default="gb300",
+                    choices=["gb300", "reference", "reference-gpu", "torch-conv"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -333,6 +363,8 @@ def main():
         return run_reference(args)
     if args.impl == "reference-gpu":
         return run_reference_gpu(args)
+    if args.impl == "torch-conv":
+        return run_torch_conv(args)
     if args.kernel_case:
         return run_kernel_case(args)
     args.warmup = max(3, args.warmup)
