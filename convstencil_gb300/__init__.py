@@ -166,6 +166,10 @@ def lib() -> ctypes.CDLL:
     L.cs_kernel_launch_count.restype = ctypes.c_longlong
     L.cs_version.restype = ctypes.c_char_p
     L.cs_device_wait_timeouts.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
+    L.cs_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                  ctypes.POINTER(vp), i]
+    L.cs_batch_run.argtypes = [vp, ll, vp, ctypes.POINTER(i)]
+    L.cs_batch_destroy.argtypes = [vp]
     L.cs_server_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]
     L.cs_server_submit.argtypes = [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ll)]
     L.cs_server_wait.argtypes = [vp, ll, dp, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
@@ -353,6 +357,40 @@ def _layout_from_dict(d) -> Layout:
     return L
 
 
+# -------------------------------------------------------------- batches
+class Batch:
+    """Several 2D plans (same radius, pattern, precision) advanced together,
+    one persistent launch per sweep (cs_batch_* in convstencil.h). ``a`` and
+    ``b`` are the per-plan ping-pong device buffers (torch tensors or
+    pointers); keep them alive while the batch exists."""
+
+    def __init__(self, plans, a, b):
+        n = len(plans)
+        P = ctypes.c_void_p * n
+        self._plans = list(plans)
+        self._keep = (list(a), list(b))
+        h = ctypes.c_void_p()
+        check(lib().cs_batch_create(ctypes.byref(h), P(*[p._h for p in plans]),
+                                    P(*[_ptr(x) for x in a]), P(*[_ptr(x) for x in b]), n))
+        self._h = h
+
+    def run(self, steps: int, stream=None) -> int:
+        res = ctypes.c_int()
+        check(lib().cs_batch_run(self._h, int(steps), ctypes.c_void_p(_ptr(stream)), ctypes.byref(res)))
+        return int(res.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # -------------------------------------------------------------- serving
 class Server:
     """Continuous-batching stencil server (cs_server_* in convstencil.h).
@@ -490,6 +528,6 @@ def selfconv(w, dims: int, r: int, k: int) -> np.ndarray:
     return acc.reshape(-1)
 
 
-__all__ = ["Plan", "Server", "Layout", "Shape", "Semantics", "Precision", "Algo", "Option",
+__all__ = ["Plan", "Batch", "Server", "Layout", "Shape", "Semantics", "Precision", "Algo", "Option",
            "ConvStencilError", "gpu_1d1r", "gpu_star_1d2r_step2", "gpu_box_2d1r", "gpu_box_2d3r",
            "gpu_box_3d1r", "gpu_star_3d1r", "selfconv", "build", "lib", "kernel_launch_count"]

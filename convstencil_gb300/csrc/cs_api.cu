@@ -910,4 +910,26 @@ cs_status run_into(cs_plan *p, const void *in, void *out, void *scratch, long lo
 
 cs_status set_error(cs_status s, const char *msg) { return fail(s, "%s", msg); }
 
+struct PlanFacts {
+    int dims, radius, pattern, steps_per_sweep;
+    cs_precision prec;
+    GridView view;
+    long long origin;
+    const Weights *w;
+};
+
+bool plan_facts(const cs_plan *p, PlanFacts *f)
+{
+    if (!p || !f) return false;
+    f->dims = p->dims;
+    f->radius = p->radius;
+    f->pattern = p->pattern;
+    f->steps_per_sweep = p->steps_per_sweep;
+    f->prec = p->prec;
+    f->view = p->view;
+    f->origin = p->layout.origin;
+    f->w = &p->w;
+    return true;
+}
+
 }  // namespace cs

@@ -196,6 +196,22 @@ CS_API cs_status cs_gpu_box_3d1r(const double *in, double *out, const double *pa
 CS_API cs_status cs_gpu_star_3d1r(const double *in, double *out, const double *params,
                                   int times, int input_h, int input_m, int input_n);
 
+/* ---- batches: uneven 2D grids in one persistent launch per sweep ------- */
+/* Plans of one batch share dims (2), radius, tap pattern, precision and
+ * steps per sweep; sizes, weights and layouts may differ. Every grid of the
+ * batch advances by the same number of steps; one launch per sweep covers
+ * the tiles of all grids. Per grid the arithmetic is that of the FP64 FMA or
+ * the split double-float kernel, so results equal a cs_run with that kernel
+ * bitwise. On a non-default stream, an even number of sweeps is captured
+ * into a CUDA graph on first use and replayed afterwards. Not in the
+ * reference. */
+typedef struct cs_batch cs_batch;
+CS_API cs_status cs_batch_create(cs_batch **batch, cs_plan *const *plans, void *const *a,
+                                 void *const *b, int count);
+/* *result_in_b: 1 when every grid's state is now in its b buffer. */
+CS_API cs_status cs_batch_run(cs_batch *batch, long long steps, void *stream, int *result_in_b);
+CS_API cs_status cs_batch_destroy(cs_batch *batch);
+
 /* ---- serving: continuous batching of stencil solves --------------------- */
 /* A worker thread admits requests while their device buffers fit in the HBM
  * budget and a slot is free, keeps their grids device-resident, and issues
