@@ -254,7 +254,7 @@ def run_kernel_case(args):
     w = O.seeded_weights(TAPS, WEIGHT_SEED)
     algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA,
             "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
-            "split_fma": cs.Algo.SPLIT_FMA}[args.kernel_case]
+            "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC}[args.kernel_case]
     split = args.kernel_case.startswith("split")
     p = cs.Plan(SHAPE, (m, n), w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
     p.set_option(cs.Option.ALGO, algo)
@@ -348,7 +348,7 @@ def main():
                     help="requests in the served-stream sample (0 = skip)")
     ap.add_argument("--served-rate", type=float, default=40.0, help="Poisson arrival rate (req/s)")
     ap.add_argument("--kernel-case", default=None,
-                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_mma_tma", "split_fma"],
+                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_mma_tma", "split_fma", "split_tc"],
                     help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid "
                          "(small cases for ncu captures) and exit")
     ap.add_argument("--m", type=int, default=4608)

@@ -77,6 +77,7 @@ class Algo(enum.IntEnum):
     SPLIT_MMA = 3
     SPLIT_FMA = 4
     SPLIT_MMA_TMA = 5
+    SPLIT_TC = 6
 
 
 class Option(enum.IntEnum):

@@ -253,10 +253,15 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(p->view, p->w, in, out, st);
         return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st);
     }
-    if (algo == CS_ALGO_SPLIT_MMA_TMA && cs::split_tma_layout_ok(p->view, off, in_base))
+    const bool tma_ok = cs::split_tma_layout_ok(p->view, off, in_base);
+    if (algo == CS_ALGO_SPLIT_TC && tma_ok)
+        return cs::launch_split_sweep_tc(p->view, p->w, off, p->layout.elements,
+                                         (const float2 *)in_base, (float2 *)out_base, st);
+    if (algo == CS_ALGO_SPLIT_MMA_TMA && tma_ok)
         return cs::launch_split_sweep_tma(p->view, p->w, off, p->layout.elements,
                                           (const float2 *)in_base, (float2 *)out_base, st);
-    if (algo == CS_ALGO_SPLIT_MMA_TMA) algo = CS_ALGO_SPLIT_MMA;  // buffer not TMA-aligned
+    if (algo == CS_ALGO_SPLIT_MMA_TMA || algo == CS_ALGO_SPLIT_TC)
+        algo = CS_ALGO_SPLIT_MMA;  // buffer not TMA-aligned
     const float2 *in = (const float2 *)in_base + off;
     float2 *out = (float2 *)out_base + off;
     return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, algo == CS_ALGO_SPLIT_MMA,
@@ -281,13 +286,14 @@ int size_class(const cs_plan *p)
 // no result) and the winner is remembered for plans of the same class.
 cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *out)
 {
-    int cand[3];
+    int cand[4];
     int nc = 0;
     if (p->prec == CS_PREC_SPLIT) {
         if (p->algo != CS_ALGO_AUTO || !split_mma_ok(p)) {
             *out = split_mma_ok(p) ? p->algo : CS_ALGO_SPLIT_FMA;
             return CS_OK;
         }
+        cand[nc++] = CS_ALGO_SPLIT_TC;
         cand[nc++] = CS_ALGO_SPLIT_MMA;
         cand[nc++] = CS_ALGO_SPLIT_MMA_TMA;
         cand[nc++] = CS_ALGO_SPLIT_FMA;
@@ -426,7 +432,10 @@ CS_API const char *cs_version(void) { return "convstencil_gb300 0.1 (sm_103a)"; 
 CS_API cs_status cs_device_wait_timeouts(unsigned *count, int reset)
 {
     if (!count) return fail(CS_ERR_INVALID_ARGUMENT, "count is NULL");
-    CS_CUDA(cs::split_wait_timeouts(count, reset != 0));
+    unsigned a = 0, b = 0;
+    CS_CUDA(cs::split_wait_timeouts(&a, reset != 0));
+    CS_CUDA(cs::split_tc_wait_timeouts(&b, reset != 0));
+    *count = a + b;
     return CS_OK;
 }
 
@@ -499,15 +508,17 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
     if (!p) return fail(CS_ERR_INVALID_ARGUMENT, "plan is NULL");
     switch (opt) {
     case CS_OPT_ALGO:
-        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_MMA_TMA) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
-        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_FMA || v == CS_ALGO_SPLIT_MMA_TMA) &&
+        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_TC) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
+        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_FMA || v == CS_ALGO_SPLIT_MMA_TMA ||
+             v == CS_ALGO_SPLIT_TC) &&
             p->prec != CS_PREC_SPLIT)
             return fail(CS_ERR_INVALID_ARGUMENT, "split algo needs a split-precision plan");
         if ((v == CS_ALGO_FP64_FMA || v == CS_ALGO_FP64_MMA) && p->prec != CS_PREC_FP64)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
         if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
-        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_MMA_TMA) && !split_mma_ok(p))
+        if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_MMA_TMA || v == CS_ALGO_SPLIT_TC) &&
+            !split_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
                         "split MMA serves 2D radius-3 plans of at least 8x8 on even-aligned layouts");
         p->algo = (int)v;

@@ -1,6 +1,7 @@
 // cs_internal.h — shared declarations between the host library and the kernels.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -53,15 +54,26 @@ bool split_tb_supported(int dims, int radius, int pattern);
 cudaError_t launch_split_sweep_tb(const GridView &g, int radius, int pattern, int T, const Weights &w,
                                   const float2 *in, float2 *out, cudaStream_t stream);
 bool split_mma_layout_ok(const GridView &g, long long origin);
-// Warp-specialised TMA variant of the slice kernel (cs_kernels_split_tma.cu);
+// TMA-fed variant of the mma.sync slice kernel (cs_kernels_split_tma.cu);
 // needs an even row pitch, >= 4 halo columns left of the interior (the TMA box
 // starts 16-byte aligned at x0-4), >= 3 halo rows, and a 16-byte aligned base.
 bool split_tma_layout_ok(const GridView &g, long long origin, const void *base);
 cudaError_t launch_split_sweep_tma(const GridView &g, const Weights &w, long long origin,
                                    long long elements, const float2 *in_base, float2 *out_base,
                                    cudaStream_t stream);
-// Bounded device-side waits that expired since the last reset.
+// tcgen05 slice kernel with TMEM accumulators (cs_kernels_split_tc.cu); same
+// layout conditions as the TMA variant.
+cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long origin,
+                                  long long elements, const float2 *in_base, float2 *out_base,
+                                  cudaStream_t stream);
+// 2D tensor map over a whole (hi, lo) buffer of `rows` x `ld` pairs, box_x x box_y tiles.
+cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long long ld, long long rows,
+                                    unsigned box_x, unsigned box_y);
+int device_sm_count();
+// Bounded device-side waits that expired since the last reset (TMA/mma.sync
+// kernel and tcgen05 kernel).
 cudaError_t split_wait_timeouts(unsigned *count, bool reset);
+cudaError_t split_tc_wait_timeouts(unsigned *count, bool reset);
 // Whole-buffer conversions and re-anchoring over n elements.
 cudaError_t launch_split_from_fp64(long long n, const double *src, float2 *dst, cudaStream_t stream);
 cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cudaStream_t stream);

@@ -306,7 +306,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-int sm_count()
+}  // namespace
+
+int device_sm_count()
 {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -314,7 +316,20 @@ int sm_count()
     return n > 0 ? n : 1;
 }
 
-}  // namespace
+cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long long ld, long long rows,
+                                    unsigned box_x, unsigned box_y)
+{
+    auto encode = encode_fn();
+    if (!encode) return cudaErrorNotSupported;
+    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * sizeof(float2))};
+    cuuint32_t box[2] = {box_x, box_y};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<float2 *>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
 
 bool split_tma_layout_ok(const GridView &g, long long origin, const void *base)
 {
@@ -329,18 +344,10 @@ cudaError_t launch_split_sweep_tma(const GridView &g, const Weights &w, long lon
                                    long long elements, const float2 *in_base, float2 *out_base,
                                    cudaStream_t st)
 {
-    auto encode = encode_fn();
-    if (!encode) return cudaErrorNotSupported;
     const long long ld = g.pitch[0];
     CUtensorMap map;
-    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)(elements / ld)};
-    cuuint64_t strides[1] = {(cuuint64_t)(ld * sizeof(float2))};
-    cuuint32_t box[2] = {ST_X, ST_Y};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<float2 *>(in_base), dims,
-                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    cudaError_t e = encode_split_window_map(&map, in_base, ld, elements / ld, ST_X, ST_Y);
+    if (e != cudaSuccess) return e;
     const size_t smem = sizeof(Smem) + 128;
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
@@ -350,7 +357,7 @@ cudaError_t launch_split_sweep_tma(const GridView &g, const Weights &w, long lon
     if (attr_err != cudaSuccess) return attr_err;
     const int tiles_x = (int)((g.ext[1] + MT_X - 1) / MT_X);
     const int tiles = tiles_x * (int)((g.ext[0] + MT_Y - 1) / MT_Y);
-    const int grid = std::min(tiles, 3 * sm_count());
+    const int grid = std::min(tiles, 3 * device_sm_count());
     note_launch();
     k2d_mma_tma<<<grid, kThreads, smem, st>>>(map, out_base + origin, (int)g.ext[0], (int)g.ext[1], ld,
                                              tiles_x, tiles, (int)(origin % ld), (int)(origin / ld),

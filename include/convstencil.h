@@ -80,11 +80,15 @@ typedef enum cs_algo {
     CS_ALGO_FP64_FMA = 1,  /* FP64 FMA, one FMA per non-zero tap (fewest FP64 ops) */
     CS_ALGO_FP64_MMA = 2,  /* FP64 tensor-core MMA (mma.sync m8n8k4.f64), 2x4 output blocks;
                               2D dense radius-3 kernels */
-    CS_ALGO_SPLIT_MMA = 3, /* split precision: exact 10-bit fixed-point slices on FP16
-                              tensor cores (mma.sync m16n8k16), 2D dense radius-3 kernels */
+    CS_ALGO_SPLIT_MMA = 3, /* split precision: five exact 9-bit fixed-point slices per operand on
+                              FP16 tensor cores (mma.sync m16n8k16), one exact FP32
+                              accumulator per slice level; 2D dense radius-3 kernels */
     CS_ALGO_SPLIT_FMA = 4, /* split precision: double-float arithmetic on FP32 cores */
-    CS_ALGO_SPLIT_MMA_TMA = 5 /* as CS_ALGO_SPLIT_MMA, warp-specialised: TMA tile loads and
-                                 slicing in producer warps, MMA in consumer warps */
+    CS_ALGO_SPLIT_MMA_TMA = 5, /* as CS_ALGO_SPLIT_MMA, tiles fetched by TMA (cp.async.bulk.tensor)
+                                  one tile ahead */
+    CS_ALGO_SPLIT_TC = 6 /* the same slices on fifth-generation tensor cores (tcgen05.mma,
+                            accumulators in tensor memory), TMA-fed; 2D dense radius-3 kernels
+                            on buffers with an even pitch, >= 4 halo columns, 16-byte aligned */
 } cs_algo;
 
 typedef enum cs_option {

@@ -72,7 +72,8 @@ CASES = [
 
 
 @pytest.mark.parametrize("shape,ext,steps", CASES)
-@pytest.mark.parametrize("algo", [cs.Algo.AUTO, cs.Algo.SPLIT_FMA, cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA])
+@pytest.mark.parametrize("algo", [cs.Algo.AUTO, cs.Algo.SPLIT_FMA, cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA,
+                                  cs.Algo.SPLIT_TC])
 def test_split_step_vs_oracle(shape, ext, steps, algo):
     info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
     w = O.seeded_weights(info[1], 500 + info[1])
@@ -80,7 +81,7 @@ def test_split_step_vs_oracle(shape, ext, steps, algo):
     try:
         p.set_option(cs.Option.ALGO, algo)
     except cs.ConvStencilError as e:
-        assert e.status == 2 and algo in (cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA)
+        assert e.status == 2 and algo in (cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA, cs.Algo.SPLIT_TC)
         pytest.skip("tensor-core split kernel serves 2D radius-3 plans of at least 8x8")
     x = O.splitmix_uniform(int(np.prod(ext)), 91).reshape(ext)
     buf = p.pack(x)
@@ -90,7 +91,7 @@ def test_split_step_vs_oracle(shape, ext, steps, algo):
     assert err[0] <= TOL, err
 
 
-@pytest.mark.parametrize("algo", [cs.Algo.SPLIT_FMA, cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA])
+@pytest.mark.parametrize("algo", [cs.Algo.SPLIT_FMA, cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA, cs.Algo.SPLIT_TC])
 def test_split_fused_2d_kernels(algo):
     """The reference's fused 7x7 kernels (cube of a 3x3 box, diamond of a star)."""
     for base, dense in ((O.seeded_weights(9, 3), None), (O.seeded_weights(5, 4), "star")):
@@ -111,7 +112,7 @@ def test_split_signed_weights_and_wide_range():
     w = O.seeded_weights(49, 12) - 1.0 / 49 * 0.5
     rng = np.random.default_rng(3)
     x = rng.standard_normal(ext) * np.exp(rng.uniform(-8, 8, ext))
-    for algo in (cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA, cs.Algo.SPLIT_FMA):
+    for algo in (cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA, cs.Algo.SPLIT_TC, cs.Algo.SPLIT_FMA):
         p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
         p.set_option(cs.Option.ALGO, algo)
         buf = p.pack(x)
