@@ -489,7 +489,9 @@ def main():
         ach = byts / hr["kernel_s"] / 1e9
         pk = float(peaks["hbm_gbs"])
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": pk, "unit": "GB/s",
-                "frac": round(ach / pk, 4), "traffic": profile_traffic("split_box2d3r_sweep"),
+                "frac": round(ach / pk, 4),
+                "traffic": profile_traffic("split_tc_box2d3r_sweep" if psp.algo == cs.Algo.SPLIT_TC
+                                           else "split_box2d3r_sweep"),
                 "kernel": f"split sweep ({psp.algo.name})",
                 "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic": f"16 B/pt (8 B read + 8 B write) x {M}x{N} pts per launch"}
