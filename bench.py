@@ -4,8 +4,8 @@
 One "step" is one stencil time step (one sweep of the 49-point kernel over
 the whole grid). Default: 1000 steps, the workload's full length.
 
-  value    GStencil/s of the split-precision path (FP32 hi+lo grids, exact BF16
-           slices on tensor cores), device-resident, K steps timed with CUDA
+  value    GStencil/s of the split-precision path (FP32 hi+lo grids, exact FP16
+           slices on the tcgen05 tensor cores), device-resident, K steps timed with CUDA
            events on the launching stream. The FP64 path (same GPU) is timed
            the same way and reported under "fp64"; the split result's error
            against the FP64 path is stated under "err".
@@ -18,7 +18,9 @@ the whole grid). Default: 1000 steps, the workload's full length.
            naive stencil) on the host cores, on a bounded sample.
 
 --impl reference runs the reference's CPU stencil path (the oracle port, all
-host cores) on the same workload and prints its own line.
+host cores) on the same workload and prints its own line. --configs measures
+every BASELINE configuration (FP64, split, and the reference's own kernels on
+this GPU) and prints one line per configuration.
 Under torchrun with N ranks each rank runs an independent replica (the
 reference has no multi-GPU path; replicas only), value = N * work / max time.
 """
@@ -232,6 +234,127 @@ def run_torch_conv(args):
     return 0
 
 
+
+# ------------------------------------------------- every BASELINE config
+def run_all_configs(args):
+    """One line per BASELINE configuration: this library's FP64 and split
+    paths (CUDA events on the launching stream, split error against FP64) and,
+    where the cubins exist, the reference's own kernel on the same GPU with
+    the reference's step counting (one launch = 3 steps for 2d1r and 3D, 2 for
+    1d2r). Reported numbers only; parity is the tests' job."""
+    import torch
+    import convstencil_gb300 as cs
+    from oracle import cs_oracle as O
+    from oracle import ref_gpu
+    cs.build()
+    have_ref = ref_gpu.available()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    cases = [("star2d1r", (1024, 1024), 100), ("box2d3r", (8192, 8192), 1000),
+             ("1d2r", (10_240_000,), 1000), ("star3d1r", (512, 512, 512), 200),
+             ("box3d1r", (512, 512, 512), 200)]
+    if args.configs_quick:
+        cases = [(s, e, max(6, k // 10)) for s, e, k in cases]
+
+    def timed(plan, a, b, steps):
+        plan.run(a, b, 2, stream=stream)  # warm-up (runs the tuner)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        in_b = plan.run(a, b, steps, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3, in_b
+
+    for shape, ext, steps in cases:
+        info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
+        pts = float(np.prod(ext))
+        x = O.splitmix_uniform(int(pts), GRID_SEED).reshape(ext)
+        w = O.seeded_weights(info[1], WEIGHT_SEED)
+        line = {"config": shape, "extent": list(ext), "time_steps": steps}
+        p64 = cs.Plan(shape, ext, w)
+        host = p64.pack(x)
+        a = torch.from_numpy(host).cuda()
+        b = torch.zeros_like(a)
+        t64, in_b = timed(p64, a, b, steps)
+        # the timed run started from the state after the warm-up: redo from x for the error
+        a.copy_(torch.from_numpy(host))
+        b.zero_()
+        in_b = p64.run(a, b, steps, stream=stream)
+        r64 = (b if in_b else a).clone()
+        line["fp64"] = {"gstencil_s": round(pts * steps / t64 / 1e9, 3), "algo": p64.algo.name}
+        psp = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT)
+        raw = torch.from_numpy(host).cuda()
+        sa = torch.zeros(psp.elements * 2, dtype=torch.float32, device="cuda")
+        sb = torch.zeros_like(sa)
+        psp.split_from_fp64(raw, sa, stream=stream)
+        s0 = sa.clone()
+        tsp, _ = timed(psp, sa, sb, steps)
+        sa.copy_(s0)
+        sb.zero_()
+        in_b = psp.run(sa, sb, steps, stream=stream)
+        psp.split_to_fp64(sb if in_b else sa, raw, stream=stream)
+        torch.cuda.synchronize()
+        d = (raw - r64).abs()
+        scale = float(r64.abs().max())
+        den = torch.clamp(r64.abs(), min=scale * 1e-3)
+        line["split"] = {"gstencil_s": round(pts * steps / tsp / 1e9, 3), "algo": psp.algo.name,
+                         "time_block": psp.time_block,
+                         "max_rel_err_vs_fp64": float((d / den).max()),
+                         "speedup_vs_fp64": round(t64 / tsp, 2)}
+        del a, b, r64, raw, sa, sb, s0
+        if have_ref:
+            try:
+                line["reference_gpu"] = _reference_config(ref_gpu, O, shape, ext, steps)
+            except ValueError as e:
+                line["reference_gpu"] = {"unavailable": str(e)}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def _reference_config(ref_gpu, O, shape, ext, steps):
+    """The reference's own kernel for one configuration; weights are seeded
+    arrays of the wrapper's parameter count (timing only)."""
+    x = O.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
+    if shape in ("star2d1r", "box2d3r"):
+        m, n = ext
+        g = np.zeros((m + 6, n + 8))
+        g[3:m + 3, 4:n + 4] = x
+        per = 3 if shape == "star2d1r" else 1
+        w49 = O.selfconv(O.star2d1r_to_dense(O.seeded_weights(5, WEIGHT_SEED)), 2, 1, 3) \
+            if per == 3 else O.seeded_weights(49, WEIGHT_SEED)
+        launches = steps // per
+        ref_gpu.box_2d(g, w49, 2, m, n)
+        _, secs = ref_gpu.box_2d(g, w49, launches, m, n)
+        kernel = "kernel2d (gpu_box_2d1r, 3 fused steps per launch)" if per == 3 else "kernel2d (gpu_box_2d3r)"
+    elif shape == "1d2r":
+        (n,) = ext
+        g = np.zeros(n + 8)
+        g[4:n + 4] = x
+        per, launches = 2, steps // 2
+        ref_gpu.one_d2r(g, O.seeded_weights(9, WEIGHT_SEED), 2, n)
+        _, secs = ref_gpu.one_d2r(g, O.seeded_weights(9, WEIGHT_SEED), launches, n)
+        kernel = "gpu_star_1d2r_step2_kernel (2 fused steps per launch)"
+    else:
+        h, m, n = ext
+        g = np.zeros((h + 6, m + 6, n + 6))
+        g[3:h + 3, 3:m + 3, 3:n + 3] = x
+        per, launches = 3, steps // 3
+        if shape == "box3d1r":
+            p = O.seeded_weights(196, WEIGHT_SEED)
+            ref_gpu.box_3d(g, p, 1, h, m, n)
+            _, secs = ref_gpu.box_3d(g, p, launches, h, m, n)
+            kernel = "gpu_box_3d1r_kernel (3 fused steps per launch)"
+        else:
+            p = O.seeded_weights(44, WEIGHT_SEED)
+            ref_gpu.star_3d(g, p, 1, h, m, n)
+            _, secs = ref_gpu.star_3d(g, p, launches, h, m, n)
+            kernel = "gpu_star_3d1r_step3_kernel (3 fused steps per launch)"
+    pts = float(np.prod(ext))
+    return {"gstencil_s": round(pts * per * launches / secs / 1e9, 3), "kernel": kernel,
+            "launches": launches, "note": "reference step counting; timed with CUDA events, "
+                                          "one Python driver-API launch per kernel"}
+
 # ------------------------------------------------------------ pipe peaks
 def run_pipe_peaks():
     """FP64 / FP32 / tensor pipe issue rates (convstencil_gb300/csrc/peaks/pipe_peaks.cu)."""
@@ -354,11 +477,16 @@ def main():
     ap.add_argument("--m", type=int, default=4608)
     ap.add_argument("--n", type=int, default=4608)
     ap.add_argument("--sweeps", type=int, default=4)
+    ap.add_argument("--configs", action="store_true",
+                    help="measure every BASELINE configuration (FP64, split, reference kernels) and exit")
+    ap.add_argument("--configs-quick", action="store_true", help="with --configs: a tenth of the steps")
     ap.add_argument("--pipe-peaks", action="store_true",
                     help="build and run the arithmetic-pipe microbenchmark and exit")
     args = ap.parse_args()
     if args.pipe_peaks:
         return run_pipe_peaks()
+    if args.configs:
+        return run_all_configs(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.impl == "reference-gpu":
