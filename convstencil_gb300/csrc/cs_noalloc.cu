@@ -24,7 +24,7 @@ cs_status set_error(cs_status s, const char *msg);
 namespace {
 
 constexpr size_t kScratchBytes = size_t(16) << 20;  // 16 MiB: 2,097,152 grid points
-__device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
