@@ -257,7 +257,7 @@ def run_all_configs(args):
         cases = [(s, e, max(6, k // 10)) for s, e, k in cases]
 
     def timed(plan, a, b, steps):
-        plan.run(a, b, 2, stream=stream)  # warm-up (runs the tuner)
+        plan.run(a, b, min(steps, 100), stream=stream)  # warm-up: tuner, and graphs of small grids
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)

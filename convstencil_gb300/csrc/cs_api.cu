@@ -30,6 +30,9 @@ namespace cs {
 static std::atomic<long long> g_launches{0};
 void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+constexpr int kGraphBlockSweeps = 32;             // sweeps per replayed graph block (about)
+constexpr long long kGraphMaxPoints = 8LL << 20;  // grids of up to 8M points replay graphs
+
 }  // namespace cs
 
 using cs::GridView;
@@ -223,6 +226,15 @@ struct cs_plan {
     int time_block = 0;            // split FMA: steps per launch (0 = tuner)
     int last_time_block = 1;
     long long reanchor = 100;
+    // Small grids: blocks of sweeps replayed as CUDA graphs (see cs_run).
+    std::mutex graph_mu;
+    std::map<std::tuple<const void *, const void *, int, int, int>, cudaGraphExec_t> graphs;
+    cudaStream_t capture_stream = nullptr;
+    ~cs_plan()
+    {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+    }
 };
 
 namespace {
@@ -595,18 +607,88 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
     void *buf[2] = {a, b};
     int cur = 0;
     const long long off = p->layout.origin;
-    for (long long i = 0; i < sweeps;) {
-        const int t = (int)std::min<long long>(tb, sweeps - i);
-        cudaError_t e;
+    // One launch of t sweeps from buf[c] to buf[c ^ 1] on stream `on`.
+    auto one_launch = [&](int t, int c, cudaStream_t on) -> cudaError_t {
         if (t >= 2)
-            e = cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w,
-                                          (const float2 *)buf[cur] + off, (float2 *)buf[cur ^ 1] + off, st);
-        else
-            e = launch_sweep(p, algo, buf[cur], buf[cur ^ 1], st);
+            return cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w,
+                                             (const float2 *)buf[c] + off, (float2 *)buf[c ^ 1] + off, on);
+        return launch_sweep(p, algo, buf[c], buf[c ^ 1], on);
+    };
+    auto reanchor_after = [&](long long start, long long done) {
+        return p->prec == CS_PREC_SPLIT && p->reanchor > 0 && done / p->reanchor != start / p->reanchor;
+    };
+    // Small grids spend a noticeable share of each sweep on launch gaps, so
+    // blocks of an even number of launches are captured once as a CUDA graph
+    // and replayed: same kernels, same order, same re-anchoring points, so the
+    // result is bitwise the one of plain launches. Not used while the caller
+    // is itself capturing `stream` (its capture records plain launches).
+    long long pts = 1;
+    for (int d = 0; d < p->dims; ++d) pts *= p->view.ext[d];
+    const int glaunches = std::max(2, (cs::kGraphBlockSweeps / tb) & ~1);
+    const long long gsweeps = (long long)glaunches * tb;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const bool graphs = pts <= cs::kGraphMaxPoints && sweeps >= 3 * gsweeps &&
+                        cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone;
+    // The graph of a block starting at buf[c], captured on the plan's private
+    // stream the first time and cached in the plan.
+    auto block_graph = [&](int c, cudaGraphExec_t *out) -> cs_status {
+        std::lock_guard<std::mutex> lk(p->graph_mu);
+        const auto key = std::make_tuple((const void *)buf[c], (const void *)buf[c ^ 1], algo, tb, glaunches);
+        auto it = p->graphs.find(key);
+        if (it != p->graphs.end()) {
+            *out = it->second;
+            return CS_OK;
+        }
+        if (!p->capture_stream)
+            CS_CUDA(cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking));
+        CS_CUDA(cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = cs::g_launches.load();
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < glaunches && e == cudaSuccess; ++k) e = one_launch(tb, c ^ (k & 1), p->capture_stream);
+        cs::note_launch(before - cs::g_launches.load());  // captured, not run: counted at each replay
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(e != cudaSuccess ? e : e2, "sweep capture");
+        }
+        cudaGraphExec_t ge = nullptr;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+        p->graphs[key] = ge;
+        *out = ge;
+        return CS_OK;
+    };
+    for (long long i = 0; i < sweeps;) {
+        // The first launch of a run is always plain, so any first-launch
+        // set-up of a kernel has happened before a capture.
+        if (graphs && i > 0 && sweeps - i >= gsweeps) {
+            bool clean = true;  // no re-anchor inside the block (one after its last launch is fine)
+            for (int k = 0; k + 1 < glaunches; ++k)
+                if (reanchor_after(i + (long long)k * tb, i + (long long)(k + 1) * tb)) clean = false;
+            if (clean) {
+                cudaGraphExec_t ge = nullptr;
+                cs_status gs = block_graph(cur, &ge);
+                if (gs != CS_OK) return gs;
+                cudaError_t e = cudaGraphLaunch(ge, st);
+                if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+                cs::note_launch(glaunches);
+                const long long done = i + gsweeps;  // even launch count: back in buf[cur]
+                if (reanchor_after(done - tb, done)) {
+                    e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[cur], st);
+                    if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
+                }
+                i = done;
+                continue;
+            }
+        }
+        const int t = (int)std::min<long long>(tb, sweeps - i);
+        cudaError_t e = one_launch(t, cur, st);
         if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         cur ^= 1;
         const long long done = i + t;
-        if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && done / p->reanchor != i / p->reanchor) {
+        if (reanchor_after(i, done)) {
             e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[cur], st);
             if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
         }
