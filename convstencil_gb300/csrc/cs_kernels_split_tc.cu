@@ -221,6 +221,29 @@ __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map
         : "memory");
 }
 
+// The MMAs of one tile: window row offset I, input digit D. Descriptor
+// addresses advance in 16-byte units: digit planes are PL halves apart, row
+// offsets one plane row, B_i matrices NCOL * 16 halves.
+template <int I, int D>
+__device__ __forceinline__ void tile_mma(unsigned d_base, unsigned long long a0, unsigned long long b0)
+{
+    constexpr unsigned long long a_off = ((unsigned long long)D * PL * 2 + I * kRowBytes) >> 4;
+    constexpr unsigned long long b_off = ((unsigned long long)I * NCOL * 16 * 2) >> 4;
+    static_assert(((unsigned long long)D * PL * 2 + I * kRowBytes) % 16 == 0 && (NCOL * 16 * 2) % 16 == 0,
+                  "descriptor offsets must be 16-byte multiples");
+    mma_f16(d_base + (unsigned)(NLV * D), a0 + a_off, b0 + b_off, instr_desc(NLV * (kDigits - D)),
+            (I | D) != 0 ? 1u : 0u);
+    if constexpr (D + 1 < kDigits)
+        tile_mma<I, D + 1>(d_base, a0, b0);
+    else if constexpr (I + 1 < NOFF)
+        tile_mma<I + 1, 0>(d_base, a0, b0);
+}
+
+__device__ __forceinline__ void issue_tile_mmas(unsigned d_base, unsigned long long a0, unsigned long long b0)
+{
+    tile_mma<0, 0>(d_base, a0, b0);
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
     k2d_tc(const __grid_constant__ CUtensorMap tmap, float2 *__restrict__ out, int m, int n,
            long long ld, int tiles_x, int tiles, int map_x, int map_y, SliceWeights sw)
@@ -292,24 +315,19 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else if (warp == kWarpMma) {
         // ------------------------------------------------ MMA issuer
+        const unsigned long long a_desc_buf0 = smem_desc(smem_addr(S.planes[0][0]), 16, R * kRowBytes);
+        const unsigned long long a_desc_buf1 = smem_desc(smem_addr(S.planes[1][0]), 16, R * kRowBytes);
+        const unsigned long long b_desc0 = smem_desc(smem_addr(S.bmat[0]), 128, 256);
         if (lane == 0) {
             for (int it = 0; it < my_tiles; ++it) {
                 const int buf = it & 1, use = it >> 1;
                 if (!mbar_wait(bar2(S.planes_full, buf), use & 1, abort)) break;
                 if (!mbar_wait(bar2(S.acc_empty, buf), (use & 1) ^ 1, abort)) break;
                 tc_fence_after();
-                const unsigned d_base = tmem + (unsigned)(kAccStride * buf);
-#pragma unroll 1
-                for (int i = 0; i < NOFF; ++i) {
-                    const unsigned long long bd = smem_desc(smem_addr(S.bmat[i]), 128, 256);
-#pragma unroll
-                    for (int d = 0; d < kDigits; ++d) {
-                        const unsigned long long ad =
-                            smem_desc(smem_addr(S.planes[buf][d]) + i * kRowBytes, 16, R * kRowBytes);
-                        mma_f16(d_base + (unsigned)(NLV * d), ad, bd, instr_desc(NLV * (kDigits - d)),
-                                (i | d) != 0 ? 1u : 0u);
-                    }
-                }
+                // The issuing thread stalls on every MMA until the tensor core
+                // takes it, so nothing else sits between them: all 50 are
+                // unrolled, each descriptor one add of a compile-time offset.
+                issue_tile_mmas(tmem + (unsigned)(kAccStride * buf), buf ? a_desc_buf1 : a_desc_buf0, b_desc0);
                 mma_commit(bar2(S.planes_empty, buf));  // planes may be overwritten
                 mma_commit(bar2(S.acc_full, buf));      // accumulator ready
                 committed = it + 1;
