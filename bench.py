@@ -253,6 +253,11 @@ def run_all_configs(args):
     cases = [("star2d1r", (1024, 1024), 100), ("box2d3r", (8192, 8192), 1000),
              ("1d2r", (10_240_000,), 1000), ("star3d1r", (512, 512, 512), 200),
              ("box3d1r", (512, 512, 512), 200)]
+    if args.all_shapes:
+        big2, big3 = (8192, 8192), (512, 512, 512)
+        cases = [("1d1r", (10_240_000,), 200), ("1d2r", (10_240_000,), 200),
+                 ("star2d1r", big2, 100), ("box2d1r", big2, 100), ("star2d3r", big2, 40),
+                 ("box2d3r", big2, 40), ("star3d1r", big3, 40), ("box3d1r", big3, 20)]
     if args.configs_quick:
         cases = [(s, e, max(6, k // 10)) for s, e, k in cases]
 
@@ -303,7 +308,7 @@ def run_all_configs(args):
                          "max_rel_err_vs_fp64": float((d / den).max()),
                          "speedup_vs_fp64": round(t64 / tsp, 2)}
         del a, b, r64, raw, sa, sb, s0
-        if have_ref:
+        if have_ref and not args.all_shapes:
             try:
                 line["reference_gpu"] = _reference_config(ref_gpu, O, shape, ext, steps)
             except ValueError as e:
@@ -480,6 +485,8 @@ def main():
     ap.add_argument("--configs", action="store_true",
                     help="measure every BASELINE configuration (FP64, split, reference kernels) and exit")
     ap.add_argument("--configs-quick", action="store_true", help="with --configs: a tenth of the steps")
+    ap.add_argument("--all-shapes", action="store_true",
+                    help="with --configs: the eight shapes at 8192^2 / 10,240,000 / 512^3 instead")
     ap.add_argument("--pipe-peaks", action="store_true",
                     help="build and run the arithmetic-pipe microbenchmark and exit")
     args = ap.parse_args()
