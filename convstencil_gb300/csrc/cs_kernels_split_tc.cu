@@ -28,10 +28,12 @@
 //     first 32 (5-d) rows of one K-major matrix) and the accumulator starts
 //     at TMEM column 32 d, so one MMA feeds levels d..4 at once: per tile
 //     10 offsets x 5 digits = 50 MMAs into 160 FP32 columns.
-//   * Measured on GB300, one M = 128, K = 16 MMA occupies the tensor core
-//     for about 128 cycles whatever N (<= 256) is, so the tile shape is
-//     chosen to serve as many outputs per MMA as shared memory allows:
+//   * The tile shape serves as many outputs per MMA as shared memory allows:
 //     4 rows per group give 4096 outputs per 50 MMAs (2 rows: 2048 per 40).
+//     The issuing thread stalls on each MMA until the tensor core accepts
+//     it, so the 50 MMAs are unrolled with compile-time descriptor offsets
+//     (measured on GB300: 56 cycles per MMA for this N = 160..32 sequence,
+//     70 with the descriptors computed in the loop).
 //   * One persistent CTA per SM (about 188 KB of shared memory) with warp
 //     roles joined by mbarriers: one warp issues the TMA window loads, one
 //     thread issues the MMAs (tcgen05.mma issue blocks while the tensor
