@@ -265,7 +265,12 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(p->view, p->w, in, out, st);
         return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st);
     }
-    const bool tma_ok = cs::split_tma_layout_ok(p->view, off, in_base);
+    // The tensor-core split kernels store float4 (two points) at even element
+    // offsets, so they need a 16-byte aligned output base; the TMA-fed ones
+    // also a 16-byte aligned input base. Otherwise the double-float kernel
+    // (8-byte accesses only) runs.
+    const bool out16 = (reinterpret_cast<uintptr_t>(out_base) % 16) == 0;
+    const bool tma_ok = out16 && cs::split_tma_layout_ok(p->view, off, in_base);
     if (algo == CS_ALGO_SPLIT_TC && tma_ok)
         return cs::launch_split_sweep_tc(p->view, p->w, off, p->layout.elements,
                                          (const float2 *)in_base, (float2 *)out_base, st);
@@ -274,6 +279,7 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
                                           (const float2 *)in_base, (float2 *)out_base, st);
     if (algo == CS_ALGO_SPLIT_MMA_TMA || algo == CS_ALGO_SPLIT_TC)
         algo = CS_ALGO_SPLIT_MMA;  // buffer not TMA-aligned
+    if (algo == CS_ALGO_SPLIT_MMA && !out16) algo = CS_ALGO_SPLIT_FMA;
     const float2 *in = (const float2 *)in_base + off;
     float2 *out = (float2 *)out_base + off;
     return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, algo == CS_ALGO_SPLIT_MMA,
@@ -591,6 +597,8 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
 {
     if (!p || !a || !b) return fail(CS_ERR_INVALID_ARGUMENT, "NULL plan or buffer");
     if (a == b) return fail(CS_ERR_INVALID_ARGUMENT, "ping-pong buffers must differ");
+    if (reinterpret_cast<uintptr_t>(a) % 8 || reinterpret_cast<uintptr_t>(b) % 8)
+        return fail(CS_ERR_INVALID_ARGUMENT, "grid buffers must be 8-byte aligned (double / float2 elements)");
     long long sweeps = 0;
     cs_status s = cs_plan_sweeps(p, steps, &sweeps);
     if (s != CS_OK) return s;
@@ -968,6 +976,8 @@ size_t plan_bytes(const cs_plan *p) { return p->layout.bytes; }
 cs_status run_into(cs_plan *p, const void *in, void *out, void *scratch, long long steps,
                    cudaStream_t st)
 {
+    if (reinterpret_cast<uintptr_t>(in) % 8 || reinterpret_cast<uintptr_t>(out) % 8)
+        return fail(CS_ERR_INVALID_ARGUMENT, "grid buffers must be 8-byte aligned (double / float2 elements)");
     long long sweeps = 0;
     cs_status s = cs_plan_sweeps(p, steps, &sweeps);
     if (s != CS_OK) return s;

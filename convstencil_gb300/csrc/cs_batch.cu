@@ -268,6 +268,9 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
     for (int i = 0; i < count; ++i) {
         if (!plans[i] || !a[i] || !b[i] || a[i] == b[i] || !cs::plan_facts(plans[i], &f[i]))
             return cs::set_error(CS_ERR_INVALID_ARGUMENT, "bad plan or buffer in batch");
+        if (reinterpret_cast<uintptr_t>(a[i]) % 8 || reinterpret_cast<uintptr_t>(b[i]) % 8)
+            return cs::set_error(CS_ERR_INVALID_ARGUMENT,
+                                 "grid buffers must be 8-byte aligned (double / float2 elements)");
         if (f[i].dims != 2)
             return cs::set_error(CS_ERR_UNSUPPORTED, "batches pack 2D grids");
         if (f[i].radius != f[0].radius || f[i].pattern != f[0].pattern || f[i].prec != f[0].prec ||

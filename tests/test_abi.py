@@ -109,3 +109,14 @@ def test_selfconv_matches_oracle():
     np.testing.assert_allclose(cs.selfconv(w, 2, 1, 3), O.selfconv(w, 2, 1, 3), rtol=1e-14)
     w = O.seeded_weights(27, 4)
     np.testing.assert_allclose(cs.selfconv(w, 3, 1, 3), O.selfconv(w, 3, 1, 3), rtol=1e-13)
+
+
+def test_run_refuses_misaligned_grid_buffers():
+    """Elements are 8 bytes (double or (hi, lo) float pairs): buffers that are
+    not 8-byte aligned are refused before anything reaches the GPU."""
+    cs.build()
+    for prec in (cs.Precision.FP64, cs.Precision.SPLIT):
+        p = cs.Plan("box2d3r", (16, 16), np.ones(49) / 49, precision=prec)
+        with pytest.raises(cs.ConvStencilError) as e:
+            p.run(0x10004, 0x20000, 1)
+        assert e.value.status == 1 and "8-byte aligned" in str(e.value)

@@ -72,9 +72,13 @@ def test_batch_validation_without_gpu():
     p1 = cs.Plan("star2d1r", (40, 40), O.seeded_weights(5, 1))
     p2 = cs.Plan("box2d3r", (40, 40), O.seeded_weights(49, 1))
     p3 = cs.Plan("star3d1r", (8, 8, 8), O.seeded_weights(7, 1))
+    # fake device addresses (8-byte aligned): the checks fail before any use
     with pytest.raises(cs.ConvStencilError) as e:
-        cs.Batch([p1, p2], [1, 2], [3, 4])
+        cs.Batch([p1, p2], [0x1000, 0x2000], [0x3000, 0x4000])
     assert "share radius" in str(e.value)
     with pytest.raises(cs.ConvStencilError) as e:
-        cs.Batch([p3], [1], [2])
+        cs.Batch([p3], [0x1000], [0x2000])
     assert e.value.status == 2
+    with pytest.raises(cs.ConvStencilError) as e:
+        cs.Batch([p1], [0x1004], [0x2000])
+    assert "8-byte aligned" in str(e.value)

@@ -177,3 +177,29 @@ def test_time_block_option_validation():
     q = cs.Plan("star2d1r", (64, 64), O.seeded_weights(5, 1))
     with pytest.raises(cs.ConvStencilError):
         q.set_option(cs.Option.TIME_BLOCK, 2)   # FP64 plans are FP64-pipe bound: not offered
+
+
+@pytest.mark.parametrize("algo", [cs.Algo.AUTO, cs.Algo.SPLIT_TC, cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA])
+def test_split_buffers_offset_by_one_pair(algo):
+    """Grids that start one (hi, lo) pair (8 bytes) past a 16-byte boundary,
+    e.g. a view into a larger allocation: the kernels that store float4 need
+    16-byte aligned buffers, so the plan runs the double-float kernel there,
+    and the result stays within the split tolerance."""
+    ext = (96, 130)
+    w = O.seeded_weights(49, 71)
+    x = O.splitmix_uniform(ext[0] * ext[1], 72).reshape(ext)
+    p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, algo)
+    buf = p.pack(x)
+    raw = torch.from_numpy(buf).cuda()
+    big_a = torch.zeros(p.elements * 2 + 2, dtype=torch.float32, device="cuda")
+    big_b = torch.zeros_like(big_a)
+    a, b = big_a[2:], big_b[2:]
+    assert a.data_ptr() % 16 == 8 and b.data_ptr() % 16 == 8
+    p.split_from_fp64(raw, a)
+    in_b = p.run(a, b, 3)
+    out = torch.zeros_like(raw)
+    p.split_to_fp64(b if in_b else a, out)
+    torch.cuda.synchronize()
+    ref = oracle_run(p, buf, w, 3, 3)
+    assert rel_err(p.unpack(out.cpu().numpy()), p.unpack(ref))[0] <= TOL
