@@ -76,14 +76,17 @@ __global__ void __launch_bounds__(256) k1d_fma(const double *__restrict__ in,
 }
 
 // ---------------------------------------------------------------- 2D
-// CTA tile 32 x 64 outputs; thread (c, g) computes column c of rows
-// 8g .. 8g+7, sweeping the 8+2R input rows of its column window once.
-template <int R, int P>
+// CTA tile (4 RPT) x 64 outputs; thread (c, g) computes column c of rows
+// RPT g .. RPT g + RPT-1, sweeping the RPT+2R input rows of its column window
+// once. RPT = 8 (32-row tiles) normally; RPT = 4 on grids too small to give
+// every SM several 32-row tiles. Each output sums its taps in the same order
+// either way.
+template <int R, int P, int RPT>
 __global__ void __launch_bounds__(256) k2d_fma(const double *__restrict__ in,
                                                double *__restrict__ out, int m, int n,
                                                long long ld, WK<(2 * R + 1) * (2 * R + 1)> w)
 {
-    constexpr int K = 2 * R + 1, TX = 64, TY = 32, RPT = 8;
+    constexpr int K = 2 * R + 1, TX = 64, TY = 4 * RPT;
     constexpr int SX = TX + 2 * R, SY = TY + 2 * R;
     __shared__ double s[SY * SX];
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
@@ -251,9 +254,16 @@ cudaError_t go2d(const GridView &g, const Weights &w, const double *in, double *
                  cudaStream_t st)
 {
     constexpr int K = 2 * R + 1;
-    dim3 grid(ceil_div(g.ext[1], 64), ceil_div(g.ext[0], 32));
-    k2d_fma<R, P><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0],
-                                         pack<K * K>(w));
+    const unsigned gx = ceil_div(g.ext[1], 64);
+    if ((long long)gx * ceil_div(g.ext[0], 32) < 6LL * device_sm_count()) {
+        dim3 grid(gx, ceil_div(g.ext[0], 16));
+        k2d_fma<R, P, 4><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0],
+                                                pack<K * K>(w));
+    } else {
+        dim3 grid(gx, ceil_div(g.ext[0], 32));
+        k2d_fma<R, P, 8><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0],
+                                                pack<K * K>(w));
+    }
     return cudaGetLastError();
 }
 
