@@ -27,6 +27,9 @@
 #include "cs_internal.h"
 #include "cs_split_common.cuh"
 
+#include <cstring>
+#include <mutex>
+
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -69,10 +72,47 @@ __device__ __forceinline__ float2 ff_finish(float sh, float sl)
     return make_float2(h, l);
 }
 
+// ff_tap on two independent accumulators at once (f32x2). w = (wh, wh),
+// nw = (-wh, -wh), wl = (wl, wl). Per lane the operations and their
+// roundings are ff_tap's: -p is formed as (-wh) * xh, which rounds to exactly
+// the negated product, and every use of p is rewritten around it.
+__device__ __forceinline__ void ff_tap2(split::f2x &sh, split::f2x &sl, split::f2x w, split::f2x nw,
+                                        split::f2x wl, split::f2x xh, split::f2x xl)
+{
+    using namespace split;
+    const f2x np = f2_mul(nw, xh);                    // -p
+    const f2x ep = f2_fma(w, xh, np);                 // exact error of the product
+    const f2x s = f2_sub(sh, np);                     // sh + p
+    const f2x bb = f2_sub(s, sh);
+    const f2x q = f2_sub(f2_sub(sh, f2_sub(s, bb)), f2_add(np, bb));  // (sh - (s - bb)) + (p - bb)
+    sh = s;
+    sl = f2_add(sl, q);
+    sl = f2_add(sl, ep);
+    sl = f2_fma(w, xl, sl);
+    sl = f2_fma(wl, xh, sl);
+}
+
+// ff_finish on both lanes.
+__device__ __forceinline__ void ff_finish2(split::f2x sh, split::f2x sl, float2 &r0, float2 &r1)
+{
+    using namespace split;
+    const f2x s = f2_add(sh, sl);
+    const f2x bb = f2_sub(s, sh);
+    const f2x e = f2_add(f2_sub(sh, f2_sub(s, bb)), f2_sub(sl, bb));
+    f2_unpack(s, r0.x, r1.x);
+    f2_unpack(e, r0.y, r1.y);
+}
+
 template <int K>
 struct FW {
     float hi[K];
     float lo[K];
+};
+
+// Weights as packed pairs for ff_tap2.
+template <int K>
+struct FW2 {
+    split::f2x w[K], nw[K], wl[K];
 };
 
 __host__ __device__ constexpr int iabs_(int x) { return x < 0 ? -x : x; }
@@ -158,8 +198,75 @@ __global__ void __launch_bounds__(256) k2d_ff(const float2 *__restrict__ in, flo
     }
 }
 
+// Dense 3D kernels (27 or 343 taps). CTA column of 16 x 32 outputs marching
+// zc planes in z. Thread (lx, ly) computes rows ly and ly + 8 of column lx
+// together, one output per lane of
+// packed FP32 pairs. Each input plane of the ring is stored as row pairs:
+// slot s holds rows s and s + 8 of the window side by side (hi parts in one
+// array, lo parts in another), so a tap reads both outputs' inputs with one
+// 64-bit load.
 template <int R, int P>
-__global__ void __launch_bounds__(256) k3d_ff(const float2 *__restrict__ in, float2 *__restrict__ out,
+__global__ void __launch_bounds__(256) k3d_ff2(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                               int h, int m, int n, long long ldy, long long ldz, int zc,
+                                               FW2<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
+{
+    using split::f2x;
+    constexpr int K = 2 * R + 1, TX = 32, TY = 16;
+    constexpr int SX = TX + 2 * R, NS = TY / 2 + 2 * R;  // columns, row-pair slots
+    constexpr int HALF = NS * SX;                         // pairs per hi (or lo) array
+    extern __shared__ f2x ring3[];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+    const int zend = min(z0 + zc, h);
+    auto load_plane = [&](int gz) {
+        float *hi = reinterpret_cast<float *>(ring3 + ((gz + K) % K) * 2 * HALF);
+        float *lo = hi + 2 * HALF;
+        const bool zok = gz < h + R;
+        for (int idx = threadIdx.x; idx < 2 * HALF; idx += blockDim.x) {
+            const int half = idx & 1, rest = idx >> 1;
+            const int sy = rest / SX, sx = rest - sy * SX;
+            const int gy = y0 - R + sy + (TY / 2) * half, gx = x0 - R + sx;
+            const float2 v = (zok && gy < m + R && gx < n + R)
+                                 ? in[(long long)gz * ldz + (long long)gy * ldy + gx]
+                                 : make_float2(0.f, 0.f);
+            hi[idx] = v.x;
+            lo[idx] = v.y;
+        }
+    };
+    for (int gz = z0 - R; gz < z0 + R; ++gz) load_plane(gz);
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    for (int z = z0; z < zend; ++z) {
+        load_plane(z + R);
+        __syncthreads();
+        f2x sh = 0ull, sl = 0ull;
+#pragma unroll
+        for (int a = 0; a < K; ++a) {
+            const f2x *ph = ring3 + ((z - R + a + K) % K) * 2 * HALF + ly * SX + lx;
+            const f2x *pl = ph + HALF;
+#pragma unroll
+            for (int i = 0; i < K; ++i)
+#pragma unroll
+                for (int j = 0; j < K; ++j)
+                    if (tap3s<P, R>(a, i, j)) {
+                        const int t = (a * K + i) * K + j;
+                        ff_tap2(sh, sl, w.w[t], w.nw[t], w.wl[t], ph[i * SX + j], pl[i * SX + j]);
+                    }
+        }
+        float2 r0, r1;
+        ff_finish2(sh, sl, r0, r1);
+        const int x = x0 + lx, ya = y0 + ly, yb = ya + TY / 2;
+        if (x < n) {
+            if (ya < m) out[(long long)z * ldz + (long long)ya * ldy + x] = r0;
+            if (yb < m) out[(long long)z * ldz + (long long)yb * ldy + x] = r1;
+        }
+        __syncthreads();
+    }
+}
+
+// Scalar form (one output at a time per thread, float2 ring): used for the
+// sparse star and diamond patterns, where loading the planes outweighs the
+// arithmetic that the packed form halves.
+template <int R, int P>
+__global__ void __launch_bounds__(256) k3d_ff1(const float2 *__restrict__ in, float2 *__restrict__ out,
                                               int h, int m, int n, long long ldy, long long ldz, int zc,
                                               FW<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
 {
@@ -526,6 +633,25 @@ FW<K> pack_ff(const Weights &w)
     return p;
 }
 
+template <int K>
+FW2<K> pack_ff2(const Weights &w)
+{
+    FW2<K> p;
+    auto pk = [](float x) {
+        unsigned u;
+        std::memcpy(&u, &x, sizeof u);
+        return ((split::f2x)u << 32) | u;
+    };
+    for (int i = 0; i < K; ++i) {
+        const float hi = (float)w.v[i];
+        const float lo = (float)(w.v[i] - (double)hi);
+        p.w[i] = pk(hi);
+        p.nw[i] = pk(-hi);
+        p.wl[i] = pk(lo);
+    }
+    return p;
+}
+
 template <int R>
 cudaError_t go1d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
 {
@@ -547,12 +673,25 @@ template <int R, int P>
 cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
 {
     constexpr int K = 2 * R + 1;
-    constexpr int smem = K * (16 + 2 * R) * (32 + 2 * R) * (int)sizeof(float2);
-    static_assert(smem <= 48 * 1024, "3D ring exceeds the default shared-memory window");
     const int zc = 32;
     dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
-    k3d_ff<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
-                                           g.pitch[1], g.pitch[0], zc, pack_ff<K * K * K>(w));
+    if constexpr (P == PAT_DENSE) {
+        constexpr int smem = K * 2 * (8 + 2 * R) * (32 + 2 * R) * (int)sizeof(split::f2x);
+        static std::once_flag once;
+        static cudaError_t attr = cudaSuccess;
+        std::call_once(once, [] {
+            if (smem > 48 * 1024)
+                attr = cudaFuncSetAttribute(k3d_ff2<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        });
+        if (attr != cudaSuccess) return attr;
+        k3d_ff2<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
+                                                g.pitch[1], g.pitch[0], zc, pack_ff2<K * K * K>(w));
+    } else {
+        constexpr int smem = K * (16 + 2 * R) * (32 + 2 * R) * (int)sizeof(float2);
+        static_assert(smem <= 48 * 1024, "3D ring exceeds the default shared-memory window");
+        k3d_ff1<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
+                                                g.pitch[1], g.pitch[0], zc, pack_ff<K * K * K>(w));
+    }
     return cudaGetLastError();
 }
 

@@ -20,6 +20,39 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = (a - (s - bb)) + (b - bb);
 }
 
+// ---- packed FP32 pairs (f32x2): one instruction, two independent lanes,
+// each lane rounded exactly as the scalar operation would be.
+typedef unsigned long long f2x;
+
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b)
+{
+    f2x r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b)
+{
+    f2x r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b)
+{
+    f2x r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c)
+{
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2x v, float &x, float &y)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+}
+
 constexpr int kDigits = 5;       // x and w slices
 constexpr int kDigitBits = 9;    // balanced base-512 digits, |d| <= 256
 constexpr float kRadix = 512.f;

@@ -203,3 +203,22 @@ def test_split_buffers_offset_by_one_pair(algo):
     torch.cuda.synchronize()
     ref = oracle_run(p, buf, w, 3, 3)
     assert rel_err(p.unpack(out.cpu().numpy()), p.unpack(ref))[0] <= TOL
+
+
+@pytest.mark.parametrize("shape", ["box3d1r", "star3d1r"])
+def test_split_fused_3d_kernels(shape):
+    """The reference's fused 7x7x7 kernels (196 plane parameters, 44
+    octahedron cells) in split precision, against the oracle."""
+    ext = (14, 20, 37)
+    if shape == "box3d1r":
+        params = np.concatenate([O.seeded_weights(49, 80 + q) for q in range(4)]) / 4
+        dense = O.box3d_planes_to_dense(params)
+    else:
+        params = O.seeded_weights(44, 85)
+        dense = O.star3d_params_to_dense(params)
+    p = cs.Plan(shape, ext, params, semantics=cs.Semantics.FUSED, precision=cs.Precision.SPLIT)
+    x = O.splitmix_uniform(int(np.prod(ext)), 86).reshape(ext)
+    buf = p.pack(x)
+    got = split_run(p, buf, 6)          # 6 steps = 2 fused sweeps
+    ref = oracle_run(p, buf, dense, 3, 2)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
