@@ -490,11 +490,7 @@ __global__ void __launch_bounds__(256, 3) k2d_mma(const float2 *__restrict__ in,
         vmax = red[0];
 #pragma unroll
         for (int i = 1; i < 8; ++i) vmax = fmaxf(vmax, red[i]);
-        int ex = 0;
-        if (vmax > 0.f) {
-            frexpf(vmax, &ex);  // vmax < 2^ex
-            ex += 1;            // |x| / 2^ex < 1/2
-        }
+        const int ex = split::tile_exponent(vmax);
         // 2. Slice into the digit planes.
         const float to_digits = ldexpf(1.0f, kDigitBits - ex);
 #pragma unroll

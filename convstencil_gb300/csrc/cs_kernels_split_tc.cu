@@ -375,11 +375,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // (d) every slicer has read wait_ok[1] and red[] before they are reused
             asm volatile("bar.sync %0, %1;" ::"n"(kSliceBarrier), "n"(kSliceThreads) : "memory");
             if (!go) break;
-            int ex = 0;
-            if (vmax > 0.f) {
-                frexpf(vmax, &ex);  // vmax < 2^ex
-                ex += 1;            // |x| / 2^ex < 1/2
-            }
+            const int ex = split::tile_exponent(vmax);
             if (leader) S.scale_exp[it & 3] = ex;
             const float to_digits = ldexpf(1.0f, kDigitBits - ex);
 #pragma unroll

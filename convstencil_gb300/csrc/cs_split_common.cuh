@@ -95,6 +95,22 @@ __device__ __forceinline__ void slice_digits(float a, float b, float (&d)[kDigit
     d[kDigits - 1] = rintf(a + b);
 }
 
+// Scale exponent of a tile from the largest |hi| in its window: every
+// |x| / 2^ex < 1/2. Clamped below at -110 so that the slicing factor
+// 2^(kDigitBits - ex) stays finite in FP32; a tile whose values are all below
+// 2^-111 is cut relative to 2^-110, a range where the (hi, lo) format has
+// already lost its low part to underflow.
+constexpr int kMinTileExp = -110;
+__device__ __forceinline__ int tile_exponent(float vmax)
+{
+    int ex = 0;
+    if (vmax > 0.f) {
+        frexpf(vmax, &ex);  // vmax < 2^ex
+        ex = max(ex + 1, kMinTileExp);
+    }
+    return ex;
+}
+
 constexpr int MT_X = 64, MT_Y = 32;              // CTA output tile
 constexpr int SL_X = MT_X + 6, SL_Y = MT_Y + 6;  // input tile with radius-3 halo
 // Halves per slice row. 102 halves = 51 words = 19 mod 32 banks: when the

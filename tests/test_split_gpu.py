@@ -222,3 +222,26 @@ def test_split_fused_3d_kernels(shape):
     got = split_run(p, buf, 6)          # 6 steps = 2 fused sweeps
     ref = oracle_run(p, buf, dense, 3, 2)
     assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
+@pytest.mark.parametrize("algo", [cs.Algo.SPLIT_TC, cs.Algo.SPLIT_MMA, cs.Algo.SPLIT_MMA_TMA, cs.Algo.SPLIT_FMA])
+@pytest.mark.parametrize("scale,tol", [(2.0 ** -125, 1e-6), (2.0 ** 100, TOL)])
+def test_split_extreme_magnitudes(algo, scale, tol):
+    """Grids whose values sit near the bottom or the top of FP32's range.
+    The slice kernels cut each tile relative to a power-of-two scale that
+    must stay finite; near 2^-125 the (hi, lo) format itself keeps only about
+    24 bits (its low part underflows), hence the looser bar there. Checked
+    against the FP64 path on the same input."""
+    ext = (96, 130)
+    w = O.seeded_weights(49, 91)
+    x = O.splitmix_uniform(ext[0] * ext[1], 92).reshape(ext) * scale
+    p64 = cs.Plan("box2d3r", ext, w)
+    buf = p64.pack(x)
+    a = torch.from_numpy(buf).cuda()
+    b = torch.zeros_like(a)
+    ref = (b if p64.run(a, b, 3) else a).cpu().numpy()
+    p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, algo)
+    got = split_run(p, buf, 3)
+    assert np.isfinite(got).all()
+    assert rel_err(p.unpack(got), p64.unpack(ref))[1] <= tol
