@@ -245,3 +245,24 @@ def test_split_extreme_magnitudes(algo, scale, tol):
     got = split_run(p, buf, 3)
     assert np.isfinite(got).all()
     assert rel_err(p.unpack(got), p64.unpack(ref))[1] <= tol
+
+
+def test_split_tc_random_sizes_and_signed_weights():
+    """The tcgen05 kernel on seeded random grid sizes (partial tiles on both
+    edges, sizes below one tile) with mixed-sign weights, against FP64."""
+    rng = np.random.default_rng(2024)
+    for trial in range(12):
+        ext = (int(rng.integers(8, 300)), int(rng.integers(8, 300)))
+        w = rng.uniform(-1.0, 1.0, 49)
+        w /= np.abs(w).sum()
+        x = rng.uniform(-1.0, 1.0, ext)
+        p64 = cs.Plan("box2d3r", ext, w)
+        buf = p64.pack(x)
+        a = torch.from_numpy(buf).cuda()
+        b = torch.zeros_like(a)
+        ref = (b if p64.run(a, b, 4) else a).cpu().numpy()
+        p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+        p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+        got = split_run(p, buf, 4)
+        err = rel_err(p.unpack(got), p64.unpack(ref))
+        assert err[1] <= TOL, (ext, err)
