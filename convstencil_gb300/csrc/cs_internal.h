@@ -48,6 +48,9 @@ bool fp64_fma_supported(int dims, int radius, int pattern);
 cudaError_t launch_split_sweep(const GridView &g, int radius, int pattern, const Weights &w,
                                int use_mma, const float2 *in, float2 *out, cudaStream_t stream);
 bool split_supported(int dims, int radius, int pattern);
+// The 3D double-float sweeps (cs_kernels_split3d.cu); called by launch_split_sweep.
+cudaError_t launch_split_sweep_3d(const GridView &g, int radius, int pattern, const Weights &w,
+                                  const float2 *in, float2 *out, cudaStream_t stream);
 // Temporal blocking: T (2..4) steps per launch of the double-float kernels,
 // 2D radius 1 and 1D radius 1-2; bitwise identical to T single sweeps.
 bool split_tb_supported(int dims, int radius, int pattern);

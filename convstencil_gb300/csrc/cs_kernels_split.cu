@@ -26,6 +26,7 @@
 //    (80 = 5 k-steps of 16).
 #include "cs_internal.h"
 #include "cs_split_common.cuh"
+#include "cs_split_ff.cuh"
 
 #include <cstring>
 #include <mutex>
@@ -37,6 +38,7 @@
 namespace cs {
 namespace {
 
+using namespace ff;
 using split::kDigitBits;
 using split::kDigits;
 using split::MT_X;
@@ -50,86 +52,6 @@ using split::mma16816;
 using split::pack_h2;
 using split::slice_digits;
 using split::two_sum;
-
-// One tap of a double-float dot product: (sh, sl) += (wh + wl) * (xh + xl).
-__device__ __forceinline__ void ff_tap(float &sh, float &sl, float wh, float wl, float xh, float xl)
-{
-    const float p = wh * xh;
-    const float ep = fmaf(wh, xh, -p);  // exact error of the product
-    float s, q;
-    two_sum(sh, p, s, q);
-    sh = s;
-    sl += q;
-    sl += ep;
-    sl = fmaf(wh, xl, sl);
-    sl = fmaf(wl, xh, sl);
-}
-
-__device__ __forceinline__ float2 ff_finish(float sh, float sl)
-{
-    float h, l;
-    two_sum(sh, sl, h, l);
-    return make_float2(h, l);
-}
-
-// ff_tap on two independent accumulators at once (f32x2). w = (wh, wh),
-// nw = (-wh, -wh), wl = (wl, wl). Per lane the operations and their
-// roundings are ff_tap's: -p is formed as (-wh) * xh, which rounds to exactly
-// the negated product, and every use of p is rewritten around it.
-__device__ __forceinline__ void ff_tap2(split::f2x &sh, split::f2x &sl, split::f2x w, split::f2x nw,
-                                        split::f2x wl, split::f2x xh, split::f2x xl)
-{
-    using namespace split;
-    const f2x np = f2_mul(nw, xh);                    // -p
-    const f2x ep = f2_fma(w, xh, np);                 // exact error of the product
-    const f2x s = f2_sub(sh, np);                     // sh + p
-    const f2x bb = f2_sub(s, sh);
-    const f2x q = f2_sub(f2_sub(sh, f2_sub(s, bb)), f2_add(np, bb));  // (sh - (s - bb)) + (p - bb)
-    sh = s;
-    sl = f2_add(sl, q);
-    sl = f2_add(sl, ep);
-    sl = f2_fma(w, xl, sl);
-    sl = f2_fma(wl, xh, sl);
-}
-
-// ff_finish on both lanes.
-__device__ __forceinline__ void ff_finish2(split::f2x sh, split::f2x sl, float2 &r0, float2 &r1)
-{
-    using namespace split;
-    const f2x s = f2_add(sh, sl);
-    const f2x bb = f2_sub(s, sh);
-    const f2x e = f2_add(f2_sub(sh, f2_sub(s, bb)), f2_sub(sl, bb));
-    f2_unpack(s, r0.x, r1.x);
-    f2_unpack(e, r0.y, r1.y);
-}
-
-template <int K>
-struct FW {
-    float hi[K];
-    float lo[K];
-};
-
-// Weights as packed pairs for ff_tap2.
-template <int K>
-struct FW2 {
-    split::f2x w[K], nw[K], wl[K];
-};
-
-__host__ __device__ constexpr int iabs_(int x) { return x < 0 ? -x : x; }
-
-template <int P, int R>
-__host__ __device__ constexpr bool tap2s(int i, int j)
-{
-    return P == PAT_DENSE ? true : P == PAT_STAR ? (i == R || j == R) : (iabs_(i - R) + iabs_(j - R) <= R);
-}
-
-template <int P, int R>
-__host__ __device__ constexpr bool tap3s(int a, int i, int j)
-{
-    return P == PAT_DENSE ? true
-           : P == PAT_STAR ? ((a != R) + (i != R) + (j != R) <= 1)
-                           : (iabs_(a - R) + iabs_(i - R) + iabs_(j - R) <= R);
-}
 
 // ----------------------------------------------------------- CUDA-core forms
 template <int R>
@@ -195,123 +117,6 @@ __global__ void __launch_bounds__(256) k2d_ff(const float2 *__restrict__ in, flo
     for (int o = 0; o < RPT; ++o) {
         const int y = y0 + g * RPT + o, x = x0 + c;
         if (y < m && x < n) out[(long long)y * ld + x] = ff_finish(sh[o], sl[o]);
-    }
-}
-
-// Dense 3D kernels (27 or 343 taps). CTA column of 16 x 32 outputs marching
-// zc planes in z. Thread (lx, ly) computes rows ly and ly + 8 of column lx
-// together, one output per lane of
-// packed FP32 pairs. Each input plane of the ring is stored as row pairs:
-// slot s holds rows s and s + 8 of the window side by side (hi parts in one
-// array, lo parts in another), so a tap reads both outputs' inputs with one
-// 64-bit load.
-template <int R, int P>
-__global__ void __launch_bounds__(256) k3d_ff2(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                               int h, int m, int n, long long ldy, long long ldz, int zc,
-                                               FW2<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
-{
-    using split::f2x;
-    constexpr int K = 2 * R + 1, TX = 32, TY = 16;
-    constexpr int SX = TX + 2 * R, NS = TY / 2 + 2 * R;  // columns, row-pair slots
-    constexpr int HALF = NS * SX;                         // pairs per hi (or lo) array
-    extern __shared__ f2x ring3[];
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
-    const int zend = min(z0 + zc, h);
-    auto load_plane = [&](int gz) {
-        float *hi = reinterpret_cast<float *>(ring3 + ((gz + K) % K) * 2 * HALF);
-        float *lo = hi + 2 * HALF;
-        const bool zok = gz < h + R;
-        for (int idx = threadIdx.x; idx < 2 * HALF; idx += blockDim.x) {
-            const int half = idx & 1, rest = idx >> 1;
-            const int sy = rest / SX, sx = rest - sy * SX;
-            const int gy = y0 - R + sy + (TY / 2) * half, gx = x0 - R + sx;
-            const float2 v = (zok && gy < m + R && gx < n + R)
-                                 ? in[(long long)gz * ldz + (long long)gy * ldy + gx]
-                                 : make_float2(0.f, 0.f);
-            hi[idx] = v.x;
-            lo[idx] = v.y;
-        }
-    };
-    for (int gz = z0 - R; gz < z0 + R; ++gz) load_plane(gz);
-    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
-    for (int z = z0; z < zend; ++z) {
-        load_plane(z + R);
-        __syncthreads();
-        f2x sh = 0ull, sl = 0ull;
-#pragma unroll
-        for (int a = 0; a < K; ++a) {
-            const f2x *ph = ring3 + ((z - R + a + K) % K) * 2 * HALF + ly * SX + lx;
-            const f2x *pl = ph + HALF;
-#pragma unroll
-            for (int i = 0; i < K; ++i)
-#pragma unroll
-                for (int j = 0; j < K; ++j)
-                    if (tap3s<P, R>(a, i, j)) {
-                        const int t = (a * K + i) * K + j;
-                        ff_tap2(sh, sl, w.w[t], w.nw[t], w.wl[t], ph[i * SX + j], pl[i * SX + j]);
-                    }
-        }
-        float2 r0, r1;
-        ff_finish2(sh, sl, r0, r1);
-        const int x = x0 + lx, ya = y0 + ly, yb = ya + TY / 2;
-        if (x < n) {
-            if (ya < m) out[(long long)z * ldz + (long long)ya * ldy + x] = r0;
-            if (yb < m) out[(long long)z * ldz + (long long)yb * ldy + x] = r1;
-        }
-        __syncthreads();
-    }
-}
-
-// Scalar form (one output at a time per thread, float2 ring): used for the
-// sparse star and diamond patterns, where loading the planes outweighs the
-// arithmetic that the packed form halves.
-template <int R, int P>
-__global__ void __launch_bounds__(256) k3d_ff1(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                              int h, int m, int n, long long ldy, long long ldz, int zc,
-                                              FW<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
-{
-    constexpr int K = 2 * R + 1, TX = 32, TY = 16;
-    constexpr int SX = TX + 2 * R, SY = TY + 2 * R, PL = SX * SY;
-    extern __shared__ float2 ring2[];
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
-    const int zend = min(z0 + zc, h);
-    auto load_plane = [&](int gz) {
-        float2 *dst = ring2 + ((gz + K) % K) * PL;
-        const bool zok = gz < h + R;
-        for (int idx = threadIdx.x; idx < PL; idx += blockDim.x) {
-            const int sy = idx / SX, sx = idx - sy * SX;
-            const int gy = y0 - R + sy, gx = x0 - R + sx;
-            dst[idx] = (zok && gy < m + R && gx < n + R)
-                           ? in[(long long)gz * ldz + (long long)gy * ldy + gx]
-                           : make_float2(0.f, 0.f);
-        }
-    };
-    for (int gz = z0 - R; gz < z0 + R; ++gz) load_plane(gz);
-    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
-    for (int z = z0; z < zend; ++z) {
-        load_plane(z + R);
-        __syncthreads();
-#pragma unroll 1
-        for (int q = 0; q < 2; ++q) {
-            const int ly = ly0 + 8 * q;
-            float sh = 0.f, sl = 0.f;
-#pragma unroll
-            for (int a = 0; a < K; ++a) {
-                const float2 *pl = ring2 + ((z - R + a + K) % K) * PL + ly * SX + lx;
-#pragma unroll
-                for (int i = 0; i < K; ++i)
-#pragma unroll
-                    for (int j = 0; j < K; ++j)
-                        if (tap3s<P, R>(a, i, j)) {
-                            const float2 v = pl[i * SX + j];
-                            const int t = (a * K + i) * K + j;
-                            ff_tap(sh, sl, w.hi[t], w.lo[t], v.x, v.y);
-                        }
-            }
-            const int y = y0 + ly, x = x0 + lx;
-            if (y < m && x < n) out[(long long)z * ldz + (long long)y * ldy + x] = ff_finish(sh, sl);
-        }
-        __syncthreads();
     }
 }
 
@@ -617,37 +422,6 @@ int sm_count()
     return n > 0 ? n : 1;
 }
 
-template <int K>
-FW<K> pack_ff(const Weights &w)
-{
-    FW<K> p;
-    for (int i = 0; i < K; ++i) {
-        const float h = (float)w.v[i];
-        p.hi[i] = h;
-        p.lo[i] = (float)(w.v[i] - (double)h);
-    }
-    return p;
-}
-
-template <int K>
-FW2<K> pack_ff2(const Weights &w)
-{
-    FW2<K> p;
-    auto pk = [](float x) {
-        unsigned u;
-        std::memcpy(&u, &x, sizeof u);
-        return ((split::f2x)u << 32) | u;
-    };
-    for (int i = 0; i < K; ++i) {
-        const float hi = (float)w.v[i];
-        const float lo = (float)(w.v[i] - (double)hi);
-        p.w[i] = pk(hi);
-        p.nw[i] = pk(-hi);
-        p.wl[i] = pk(lo);
-    }
-    return p;
-}
-
 template <int R>
 cudaError_t go1d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
 {
@@ -662,32 +436,6 @@ cudaError_t go2d(const GridView &g, const Weights &w, const float2 *in, float2 *
     dim3 grid(ceil_div(g.ext[1], 64), ceil_div(g.ext[0], 32));
     k2d_ff<R, P><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0],
                                         pack_ff<K * K>(w));
-    return cudaGetLastError();
-}
-
-template <int R, int P>
-cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
-{
-    constexpr int K = 2 * R + 1;
-    const int zc = 32;
-    dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
-    if constexpr (P == PAT_DENSE) {
-        constexpr int smem = K * 2 * (8 + 2 * R) * (32 + 2 * R) * (int)sizeof(split::f2x);
-        static std::once_flag once;
-        static cudaError_t attr = cudaSuccess;
-        std::call_once(once, [] {
-            if (smem > 48 * 1024)
-                attr = cudaFuncSetAttribute(k3d_ff2<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        });
-        if (attr != cudaSuccess) return attr;
-        k3d_ff2<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
-                                                g.pitch[1], g.pitch[0], zc, pack_ff2<K * K * K>(w));
-    } else {
-        constexpr int smem = K * (16 + 2 * R) * (32 + 2 * R) * (int)sizeof(float2);
-        static_assert(smem <= 48 * 1024, "3D ring exceeds the default shared-memory window");
-        k3d_ff1<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
-                                                g.pitch[1], g.pitch[0], zc, pack_ff<K * K * K>(w));
-    }
     return cudaGetLastError();
 }
 
@@ -775,15 +523,7 @@ cudaError_t launch_split_sweep(const GridView &g, int R, int P, const Weights &w
             return go2d<3, PAT_DENSE>(g, w, in, out, st);
         }
     } else if (g.dims == 3) {
-        if (R == 1) {
-            if (P == PAT_STAR) return go3d<1, PAT_STAR>(g, w, in, out, st);
-            return go3d<1, PAT_DENSE>(g, w, in, out, st);
-        }
-        if (R == 3) {
-            if (P == PAT_STAR) return go3d<3, PAT_STAR>(g, w, in, out, st);
-            if (P == PAT_DIAMOND) return go3d<3, PAT_DIAMOND>(g, w, in, out, st);
-            return go3d<3, PAT_DENSE>(g, w, in, out, st);
-        }
+        return launch_split_sweep_3d(g, R, P, w, in, out, st);
     }
     return cudaErrorInvalidValue;
 }

@@ -1,0 +1,180 @@
+// cs_kernels_split3d.cu — the 3D double-float split sweeps (kept apart from
+// cs_kernels_split.cu so the two compile in parallel: the fused 7x7x7 forms
+// unroll 343 taps).
+#include "cs_internal.h"
+#include "cs_split_common.cuh"
+#include "cs_split_ff.cuh"
+
+#include <mutex>
+
+namespace cs {
+namespace {
+
+using namespace ff;
+
+unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+// Dense 3D kernels (27 or 343 taps). CTA column of 16 x 32 outputs marching
+// zc planes in z. Thread (lx, ly) computes rows ly and ly + 8 of column lx
+// together, one output per lane of
+// packed FP32 pairs. Each input plane of the ring is stored as row pairs:
+// slot s holds rows s and s + 8 of the window side by side (hi parts in one
+// array, lo parts in another), so a tap reads both outputs' inputs with one
+// 64-bit load.
+template <int R, int P>
+__global__ void __launch_bounds__(256) k3d_ff2(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                               int h, int m, int n, long long ldy, long long ldz, int zc,
+                                               FW2<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
+{
+    using split::f2x;
+    constexpr int K = 2 * R + 1, TX = 32, TY = 16;
+    constexpr int SX = TX + 2 * R, NS = TY / 2 + 2 * R;  // columns, row-pair slots
+    constexpr int HALF = NS * SX;                         // pairs per hi (or lo) array
+    extern __shared__ f2x ring3[];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+    const int zend = min(z0 + zc, h);
+    auto load_plane = [&](int gz) {
+        float *hi = reinterpret_cast<float *>(ring3 + ((gz + K) % K) * 2 * HALF);
+        float *lo = hi + 2 * HALF;
+        const bool zok = gz < h + R;
+        for (int idx = threadIdx.x; idx < 2 * HALF; idx += blockDim.x) {
+            const int half = idx & 1, rest = idx >> 1;
+            const int sy = rest / SX, sx = rest - sy * SX;
+            const int gy = y0 - R + sy + (TY / 2) * half, gx = x0 - R + sx;
+            const float2 v = (zok && gy < m + R && gx < n + R)
+                                 ? in[(long long)gz * ldz + (long long)gy * ldy + gx]
+                                 : make_float2(0.f, 0.f);
+            hi[idx] = v.x;
+            lo[idx] = v.y;
+        }
+    };
+    for (int gz = z0 - R; gz < z0 + R; ++gz) load_plane(gz);
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    for (int z = z0; z < zend; ++z) {
+        load_plane(z + R);
+        __syncthreads();
+        f2x sh = 0ull, sl = 0ull;
+        // Planes of the radius-3 (fused 7x7x7) kernels stay a loop: 49 taps
+        // unrolled per plane keep the code size and compile time in bounds.
+#pragma unroll(R == 1 ? K : 1)
+        for (int a = 0; a < K; ++a) {
+            const f2x *ph = ring3 + ((z - R + a + K) % K) * 2 * HALF + ly * SX + lx;
+            const f2x *pl = ph + HALF;
+#pragma unroll
+            for (int i = 0; i < K; ++i)
+#pragma unroll
+                for (int j = 0; j < K; ++j)
+                    if (tap3s<P, R>(a, i, j)) {
+                        const int t = (a * K + i) * K + j;
+                        ff_tap2(sh, sl, w.w[t], w.nw[t], w.wl[t], ph[i * SX + j], pl[i * SX + j]);
+                    }
+        }
+        float2 r0, r1;
+        ff_finish2(sh, sl, r0, r1);
+        const int x = x0 + lx, ya = y0 + ly, yb = ya + TY / 2;
+        if (x < n) {
+            if (ya < m) out[(long long)z * ldz + (long long)ya * ldy + x] = r0;
+            if (yb < m) out[(long long)z * ldz + (long long)yb * ldy + x] = r1;
+        }
+        __syncthreads();
+    }
+}
+
+// Scalar form (one output at a time per thread, float2 ring): used for the
+// sparse star and diamond patterns, where loading the planes outweighs the
+// arithmetic that the packed form halves.
+template <int R, int P>
+__global__ void __launch_bounds__(256) k3d_ff1(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                              int h, int m, int n, long long ldy, long long ldz, int zc,
+                                              FW<(2 * R + 1) * (2 * R + 1) * (2 * R + 1)> w)
+{
+    constexpr int K = 2 * R + 1, TX = 32, TY = 16;
+    constexpr int SX = TX + 2 * R, SY = TY + 2 * R, PL = SX * SY;
+    extern __shared__ float2 ring2[];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+    const int zend = min(z0 + zc, h);
+    auto load_plane = [&](int gz) {
+        float2 *dst = ring2 + ((gz + K) % K) * PL;
+        const bool zok = gz < h + R;
+        for (int idx = threadIdx.x; idx < PL; idx += blockDim.x) {
+            const int sy = idx / SX, sx = idx - sy * SX;
+            const int gy = y0 - R + sy, gx = x0 - R + sx;
+            dst[idx] = (zok && gy < m + R && gx < n + R)
+                           ? in[(long long)gz * ldz + (long long)gy * ldy + gx]
+                           : make_float2(0.f, 0.f);
+        }
+    };
+    for (int gz = z0 - R; gz < z0 + R; ++gz) load_plane(gz);
+    const int lx = threadIdx.x & 31, ly0 = threadIdx.x >> 5;
+    for (int z = z0; z < zend; ++z) {
+        load_plane(z + R);
+        __syncthreads();
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+            const int ly = ly0 + 8 * q;
+            float sh = 0.f, sl = 0.f;
+            // Planes of the radius-3 (fused 7x7x7) kernels stay a loop (see k3d_ff2).
+#pragma unroll(R == 1 ? K : 1)
+            for (int a = 0; a < K; ++a) {
+                const float2 *pl = ring2 + ((z - R + a + K) % K) * PL + ly * SX + lx;
+#pragma unroll
+                for (int i = 0; i < K; ++i)
+#pragma unroll
+                    for (int j = 0; j < K; ++j)
+                        if (tap3s<P, R>(a, i, j)) {
+                            const float2 v = pl[i * SX + j];
+                            const int t = (a * K + i) * K + j;
+                            ff_tap(sh, sl, w.hi[t], w.lo[t], v.x, v.y);
+                        }
+            }
+            const int y = y0 + ly, x = x0 + lx;
+            if (y < m && x < n) out[(long long)z * ldz + (long long)y * ldy + x] = ff_finish(sh, sl);
+        }
+        __syncthreads();
+    }
+}
+
+template <int R, int P>
+cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
+{
+    constexpr int K = 2 * R + 1;
+    const int zc = 32;
+    dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
+    if constexpr (P == PAT_DENSE) {
+        constexpr int smem = K * 2 * (8 + 2 * R) * (32 + 2 * R) * (int)sizeof(split::f2x);
+        static std::once_flag once;
+        static cudaError_t attr = cudaSuccess;
+        std::call_once(once, [] {
+            if (smem > 48 * 1024)
+                attr = cudaFuncSetAttribute(k3d_ff2<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        });
+        if (attr != cudaSuccess) return attr;
+        k3d_ff2<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
+                                                g.pitch[1], g.pitch[0], zc, pack_ff2<K * K * K>(w));
+    } else {
+        constexpr int smem = K * (16 + 2 * R) * (32 + 2 * R) * (int)sizeof(float2);
+        static_assert(smem <= 48 * 1024, "3D ring exceeds the default shared-memory window");
+        k3d_ff1<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2],
+                                                g.pitch[1], g.pitch[0], zc, pack_ff<K * K * K>(w));
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_split_sweep_3d(const GridView &g, int R, int P, const Weights &w, const float2 *in,
+                                  float2 *out, cudaStream_t st)
+{
+    if (R == 1) {
+        if (P == PAT_STAR) return go3d<1, PAT_STAR>(g, w, in, out, st);
+        return go3d<1, PAT_DENSE>(g, w, in, out, st);
+    }
+    if (R == 3) {
+        if (P == PAT_STAR) return go3d<3, PAT_STAR>(g, w, in, out, st);
+        if (P == PAT_DIAMOND) return go3d<3, PAT_DIAMOND>(g, w, in, out, st);
+        return go3d<3, PAT_DENSE>(g, w, in, out, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace cs
