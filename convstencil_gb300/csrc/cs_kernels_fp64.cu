@@ -20,6 +20,8 @@
 //    plan's tuner only picks it if it measures faster.
 #include "cs_internal.h"
 
+#include <algorithm>
+
 #include <cstdio>
 
 namespace cs {
@@ -249,6 +251,19 @@ WK<K> pack(const Weights &w)
 
 unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// Planes per CTA of the z-marching 3D kernels: 32 on large grids; fewer on
+// small ones, so that the grid still gives every SM several CTAs (a CTA
+// marches its planes one after another, so a small grid with 32-plane
+// columns would leave most SMs idle and make each sweep a long serial chain).
+int z_chunk(const GridView &g)
+{
+    const long long cols = (long long)ceil_div(g.ext[2], 32) * ceil_div(g.ext[1], 16);
+    const long long want = 4LL * device_sm_count();
+    long long zc = (g.ext[0] * cols + want - 1) / want;
+    return (int)std::max(1LL, std::min(32LL, zc));
+}
+
+
 template <int R, int P>
 cudaError_t go2d(const GridView &g, const Weights &w, const double *in, double *out,
                  cudaStream_t st)
@@ -274,7 +289,7 @@ cudaError_t go3d(const GridView &g, const Weights &w, const double *in, double *
     constexpr int K = 2 * R + 1;
     constexpr int smem = k3d_smem_bytes<R>();  // <= 46,816 B: no opt-in needed
     static_assert(smem <= 48 * 1024, "3D ring exceeds the default shared-memory window");
-    const int zc = 32;
+    const int zc = z_chunk(g);
     dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
     k3d_fma<R, P><<<grid, 256, smem, st>>>(in, out, (int)g.ext[0], (int)g.ext[1],
                                             (int)g.ext[2], g.pitch[1], g.pitch[0], zc,

@@ -5,6 +5,7 @@
 #include "cs_split_common.cuh"
 #include "cs_split_ff.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace cs {
@@ -13,6 +14,19 @@ namespace {
 using namespace ff;
 
 unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+// Planes per CTA of the z-marching 3D kernels: 32 on large grids; fewer on
+// small ones, so that the grid still gives every SM several CTAs (a CTA
+// marches its planes one after another, so a small grid with 32-plane
+// columns would leave most SMs idle and make each sweep a long serial chain).
+int z_chunk(const GridView &g)
+{
+    const long long cols = (long long)ceil_div(g.ext[2], 32) * ceil_div(g.ext[1], 16);
+    const long long want = 4LL * device_sm_count();
+    long long zc = (g.ext[0] * cols + want - 1) / want;
+    return (int)std::max(1LL, std::min(32LL, zc));
+}
+
 
 // Dense 3D kernels (27 or 343 taps). CTA column of 16 x 32 outputs marching
 // zc planes in z. Thread (lx, ly) computes rows ly and ly + 8 of column lx
@@ -138,7 +152,7 @@ template <int R, int P>
 cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *out, cudaStream_t st)
 {
     constexpr int K = 2 * R + 1;
-    const int zc = 32;
+    const int zc = z_chunk(g);
     dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
     if constexpr (P == PAT_DENSE) {
         constexpr int smem = K * 2 * (8 + 2 * R) * (32 + 2 * R) * (int)sizeof(split::f2x);

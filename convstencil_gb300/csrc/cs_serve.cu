@@ -8,7 +8,9 @@
 //   * execution: every scheduling turn issues one chunk of sweeps per active
 //     request on that request's stream (a pool of streams), so the work of
 //     different requests overlaps on the device; a chunk is captured once as a
-//     CUDA graph and replayed;
+//     CUDA graph and replayed. Small requests (a few ms of work or less) are
+//     issued whole, chunk after chunk, on high-priority streams, so the
+//     hardware runs their kernels ahead of the large requests' chunks;
 //   * completion: the result goes to a pinned host buffer, the device memory is
 //     released (making room for queued requests), the latency is recorded.
 // Kernel choice and FP64 re-anchoring points depend only on the request, never
@@ -31,6 +33,11 @@
 #include <vector>
 
 namespace {
+
+// Requests below this many tap-updates (about 4 ms of FP64 FMA work) are
+// issued whole on a high-priority stream: their latency is then their own
+// GPU time, not a scheduling turn per chunk behind the large requests.
+constexpr double kSmallWork = 2e9;
 
 double now_s()
 {
@@ -93,6 +100,7 @@ struct Request {
     cudaStream_t stream = nullptr;
     cudaEvent_t chunk_ev = nullptr, done_ev = nullptr;
     bool chunk_pending = false;
+    bool small = false;     // little work: issued whole, on a high-priority stream
     cudaGraphExec_t graph = nullptr;
     long long graph_steps = 0;
     int full_chunks = 0;
@@ -108,7 +116,8 @@ struct Request {
 struct cs_server {
     cs_server_config cfg{};
     int device = 0;
-    std::vector<cudaStream_t> streams;
+    std::vector<cudaStream_t> streams;        // large requests (lowest priority)
+    std::vector<cudaStream_t> fast_streams;   // small requests (highest priority)
     PinnedPool pinned;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -123,7 +132,8 @@ struct cs_server {
     std::vector<double> latencies;
     long long completed = 0, failed = 0;
     double point_steps = 0, t_first = 0, t_last = 0;
-    int rr = 0;
+    int rr = 0, rr_fast = 0;
+    int sm_count = 1;
 };
 
 namespace {
@@ -152,7 +162,8 @@ void release_device(Request *r)
 bool start_request(cs_server *s, Request *r)
 {
     const size_t b = r->layout.bytes;
-    r->stream = s->streams[s->rr++ % s->streams.size()];
+    r->stream = r->small ? s->fast_streams[s->rr_fast++ % s->fast_streams.size()]
+                         : s->streams[s->rr++ % s->streams.size()];
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaMallocAsync(&r->d[i], b, r->stream);
     if (e == cudaSuccess && r->prec == CS_PREC_SPLIT) e = cudaMallocAsync(&r->stage, b, r->stream);
@@ -198,7 +209,21 @@ cs_status issue_steps(Request *r, long long steps)
     return CS_OK;
 }
 
-// One scheduling turn for an active request: the next chunk of steps.
+// Result to the pinned host buffer; completion is seen through done_ev.
+void finish_request(Request *r)
+{
+    const void *res = r->d[r->cur];
+    if (r->prec == CS_PREC_SPLIT) {
+        cs_split_to_fp64(r->plan, res, (double *)r->stage, r->stream);
+        res = r->stage;
+    }
+    cudaMemcpyAsync(r->host, res, r->layout.bytes, cudaMemcpyDeviceToHost, r->stream);
+    cudaEventRecord(r->done_ev, r->stream);
+    r->state = State::Draining;
+}
+
+// One scheduling turn for an active request: the next chunk of steps (all of
+// them for a small request).
 void advance(cs_server *s, Request *r)
 {
     if (r->chunk_pending) {
@@ -207,6 +232,22 @@ void advance(cs_server *s, Request *r)
     }
     // Chunks are whole fused sweeps: a multiple of the plan's steps per sweep.
     const long long full = std::max(1LL, s->cfg.chunk_steps / r->sweeps_per_step) * r->sweeps_per_step;
+    if (r->small) {
+        // All chunks now, back to back on the request's high-priority stream:
+        // the same kernels and re-anchoring points as chunk-by-chunk issue,
+        // without a scheduling turn between chunks.
+        while (r->issued < r->steps) {
+            const long long chunk = std::min(full, r->steps - r->issued);
+            const cs_status st = issue_steps(r, chunk);
+            if (st != CS_OK) {
+                fail_request(s, r, st, cs_last_error());
+                return;
+            }
+            r->issued += chunk;
+        }
+        finish_request(r);
+        return;
+    }
     const long long chunk = std::min(full, r->steps - r->issued);
     cs_status st = CS_OK;
     const bool graphable = s->cfg.use_graphs && chunk == full &&
@@ -241,14 +282,7 @@ void advance(cs_server *s, Request *r)
     if (chunk == full) r->full_chunks++;
     r->issued += chunk;
     if (r->issued >= r->steps) {
-        const void *res = r->d[r->cur];
-        if (r->prec == CS_PREC_SPLIT) {
-            cs_split_to_fp64(r->plan, res, (double *)r->stage, r->stream);
-            res = r->stage;
-        }
-        cudaMemcpyAsync(r->host, res, r->layout.bytes, cudaMemcpyDeviceToHost, r->stream);
-        cudaEventRecord(r->done_ev, r->stream);
-        r->state = State::Draining;
+        finish_request(r);
     } else {
         cudaEventRecord(r->chunk_ev, r->stream);
         r->chunk_pending = true;
@@ -372,6 +406,8 @@ CS_API cs_status cs_server_create(cs_server **out, const cs_server_config *cfg)
     auto s = std::make_unique<cs_server>();
     s->cfg = c;
     if (cudaGetDevice(&s->device) != cudaSuccess) return CS_ERR_NO_DEVICE;
+    cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+    if (s->sm_count < 1) s->sm_count = 1;
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return CS_ERR_CUDA;
     s->budget = (size_t)(c.hbm_fraction * (double)free_b);
@@ -380,10 +416,15 @@ CS_API cs_status cs_server_create(cs_server **out, const cs_server_config *cfg)
         unsigned long long keep = s->budget;  // keep freed blocks for the next admissions
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
     for (int i = 0; i < c.streams; ++i) {
-        cudaStream_t st;
-        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CS_ERR_CUDA;
+        cudaStream_t st, fast;
+        if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, least) != cudaSuccess) return CS_ERR_CUDA;
         s->streams.push_back(st);
+        if (cudaStreamCreateWithPriority(&fast, cudaStreamNonBlocking, greatest) != cudaSuccess)
+            return CS_ERR_CUDA;
+        s->fast_streams.push_back(fast);
     }
     s->worker = std::thread(worker_main, s.get());
     *out = s.release();
@@ -397,12 +438,24 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
     cs_status st = cs_plan_create(&r->plan, d->shape, d->semantics, d->precision, d->extent, d->weights,
                                   d->n_weights, nullptr);
     if (st != CS_OK) return st;
-    // A fixed kernel choice (no timing-dependent tuning) keeps results
-    // identical in any mix: the FP64 FMA kernels, and for split precision
-    // the tensor-core slice kernel where it applies.
+    // A fixed kernel choice keeps results identical in any mix and keeps the
+    // plan tuner (which times candidates synchronously) off the worker
+    // thread: the FP64 FMA kernels; for split precision the tcgen05 slice
+    // kernel where it applies (it falls back by itself on buffers it cannot
+    // use), else the double-float kernels with a fixed temporal block (their
+    // results do not depend on it).
     if (d->precision == CS_PREC_SPLIT) {
-        if (cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_SPLIT_MMA) != CS_OK)
+        // tcgen05 pays a fixed ~16 us per sweep (one 64 x 64 tile per CTA and
+        // SM, set-up of its weight matrices and TMEM); below about four tiles
+        // per SM the mma.sync slice kernel (~8 us floor) finishes sooner.
+        const long long tiles = ((d->extent[0] + 63) / 64) * ((d->extent[1] + 63) / 64);
+        const int algo = tiles >= 4LL * s->sm_count ? CS_ALGO_SPLIT_TC : CS_ALGO_SPLIT_MMA;
+        if (cs_plan_set_option(r->plan, CS_OPT_ALGO, algo) != CS_OK)
             cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_SPLIT_FMA);
+        const int tb = (d->shape == CS_SHAPE_1D1R || d->shape == CS_SHAPE_1D2R) ? 4
+                       : d->shape == CS_SHAPE_STAR2D1R                           ? 3
+                                                                                 : 2;
+        cs_plan_set_option(r->plan, CS_OPT_TIME_BLOCK, tb);
     } else {
         cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_FMA);
     }
@@ -422,6 +475,17 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
     cs_plan_get_layout(r->plan, &r->layout);
     r->prec = d->precision;
     r->steps = d->steps;
+    {
+        // Work estimate: point-sweeps times the stencil window, split precision
+        // counted at an eighth (its kernels run ~10x the FP64 rate).
+        double pts = 1, taps = 1;
+        for (int k = 0; k < r->layout.dims; ++k) {
+            pts *= (double)r->layout.extent[k];
+            taps *= 2.0 * r->layout.halo + 1.0;
+        }
+        const double work = pts * (double)sweeps1 * taps / (d->precision == CS_PREC_SPLIT ? 8.0 : 1.0);
+        r->small = work < kSmallWork;
+    }
     r->bytes = r->layout.bytes * (d->precision == CS_PREC_SPLIT ? 3 : 2);
     r->host = s->pinned.get(r->layout.bytes, &r->host_cls);
     if (!r->host) {
@@ -519,6 +583,7 @@ CS_API cs_status cs_server_destroy(cs_server *s)
         cs_plan_destroy(r->plan);
     }
     for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
+    for (cudaStream_t st : s->fast_streams) cudaStreamDestroy(st);
     delete s;
     return CS_OK;
 }
