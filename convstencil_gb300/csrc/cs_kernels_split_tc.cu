@@ -259,6 +259,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const unsigned stage_full = smem_addr(&S.stage_full), stage_empty = smem_addr(&S.stage_empty);
     auto bar2 = [](unsigned long long (&b)[2], int i) { return smem_addr(&b[i]); };
 
+    int issued = 0, committed = 0;  // window loads issued / MMA batches committed (one thread each)
     if (tid == 0) {
         mbar_init(stage_full, 1);
         mbar_init(stage_empty, kSliceWarps);
@@ -270,6 +271,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (my_tiles > 0) {  // the first window load overlaps the set-up below
+            const int ty = (int)blockIdx.x / tiles_x;
+            const int x0 = ((int)blockIdx.x - ty * tiles_x) * TX, y0 = ty * TY;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(stage_full),
+                         "r"(kStageBytes)
+                         : "memory");
+            tma_load_2d(smem_addr(S.stage), &tmap, map_x + x0 - 4, map_y + y0 - 3, stage_full);
+            issued = 1;
+        }
     }
     if (warp == kWarpTma) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -298,12 +308,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         x0 = (tile - ty * tiles_x) * TX;
         y0 = ty * TY;
     };
-    int issued = 0, committed = 0;  // window loads issued / MMA batches committed (one thread each)
 
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
-            for (int it = 0; it < my_tiles; ++it) {
+            for (int it = issued; it < my_tiles; ++it) {
                 if (!mbar_wait(stage_empty, (it & 1) ^ 1, abort)) break;
                 int x0, y0;
                 tile_origin(it, x0, y0);
