@@ -28,6 +28,17 @@ __device__ __forceinline__ void ff_tap(float &sh, float &sl, float wh, float wl,
     sl = fmaf(wl, xh, sl);
 }
 
+// ff_tap into an empty sum (sh = sl = 0): the TwoSum with zero is exact, so
+// only the product, its error and the two cross terms remain. Equal to
+// ff_tap from (0, 0) up to the sign of a zero.
+__device__ __forceinline__ void ff_first(float &sh, float &sl, float wh, float wl, float xh, float xl)
+{
+    sh = wh * xh;
+    sl = fmaf(wh, xh, -sh);
+    sl = fmaf(wh, xl, sl);
+    sl = fmaf(wl, xh, sl);
+}
+
 __device__ __forceinline__ float2 ff_finish(float sh, float sl)
 {
     float h, l;

@@ -205,6 +205,20 @@ def test_split_buffers_offset_by_one_pair(algo):
     assert rel_err(p.unpack(out.cpu().numpy()), p.unpack(ref))[0] <= TOL
 
 
+@pytest.mark.parametrize("ext", [(70, 9, 33), (40, 130, 70), (160, 256, 256), (3, 17, 31), (1, 1, 1)])
+def test_split_star3d_z_marching(ext):
+    """The 7-point star's z-marching kernel: one plane per CTA (tall, thin
+    grids), a few planes, 32 planes per CTA (large grids), ragged x/y edges
+    and a single point; signed weights. Against the oracle."""
+    w = O.seeded_weights(7, 93) - 0.1
+    p = cs.Plan("star3d1r", ext, w, precision=cs.Precision.SPLIT)
+    x = O.splitmix_uniform(int(np.prod(ext)), 94).reshape(ext) - 0.5
+    buf = p.pack(x)
+    got = split_run(p, buf, 5)
+    ref = oracle_run(p, buf, _dense("star3d1r", w), 1, 5)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
 @pytest.mark.parametrize("shape", ["box3d1r", "star3d1r"])
 def test_split_fused_3d_kernels(shape):
     """The reference's fused 7x7x7 kernels (196 plane parameters, 44
