@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I", os.path.join(ROOT, "include")]
 SOURCES = ["cs_api.cu", "cs_kernels_fp64.cu", "cs_kernels_split.cu", "cs_kernels_split3d.cu",
            "cs_kernels_split_tma.cu", "cs_kernels_split_tc.cu", "cs_ref_compat.cu", "cs_noalloc.cu",
-           "cs_batch.cu", "cs_serve.cu"]
+           "cs_batch.cu", "cs_serve.cu", "cs_kernels_split_tc3d.cu"]
 CLIS = ["convstencil_1d", "convstencil_2d", "convstencil_3d"]
 
 

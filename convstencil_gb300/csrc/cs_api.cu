@@ -255,6 +255,13 @@ bool split_mma_ok(const cs_plan *p)
            cs::split_mma_layout_ok(p->view, p->layout.origin);
 }
 
+// Split plans of 3D radius-1 stencils (27 weights) also run on the tcgen05
+// slice kernel.
+bool split_tc3d_ok(const cs_plan *p)
+{
+    return p->prec == CS_PREC_SPLIT && p->dims == 3 && p->radius == 1;
+}
+
 cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *out_base,
                          cudaStream_t st)
 {
@@ -270,6 +277,13 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
     // also a 16-byte aligned input base. Otherwise the double-float kernel
     // (8-byte accesses only) runs.
     const bool out16 = (reinterpret_cast<uintptr_t>(out_base) % 16) == 0;
+    if (p->dims == 3) {
+        if (algo == CS_ALGO_SPLIT_TC && split_tc3d_ok(p) &&
+            cs::split_tc3d_layout_ok(p->view, off, in_base, out_base))
+            return cs::launch_split_sweep_tc3d(p->view, p->w, off, p->layout.elements,
+                                               (const float2 *)in_base, (float2 *)out_base, st);
+        algo = CS_ALGO_SPLIT_FMA;
+    }
     const bool tma_ok = out16 && cs::split_tma_layout_ok(p->view, off, in_base);
     if (algo == CS_ALGO_SPLIT_TC && tma_ok)
         return cs::launch_split_sweep_tc(p->view, p->w, off, p->layout.elements,
@@ -306,7 +320,16 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
 {
     int cand[4];
     int nc = 0;
-    if (p->prec == CS_PREC_SPLIT) {
+    if (p->prec == CS_PREC_SPLIT && split_tc3d_ok(p)) {
+        // The 7-point star keeps its own double-float kernel; a pinned
+        // algorithm is either the tcgen05 kernel or the double-float one.
+        if (p->algo != CS_ALGO_AUTO || p->pattern != cs::PAT_DENSE) {
+            *out = p->algo == CS_ALGO_SPLIT_TC ? CS_ALGO_SPLIT_TC : CS_ALGO_SPLIT_FMA;
+            return CS_OK;
+        }
+        cand[nc++] = CS_ALGO_SPLIT_TC;
+        cand[nc++] = CS_ALGO_SPLIT_FMA;
+    } else if (p->prec == CS_PREC_SPLIT) {
         if (p->algo != CS_ALGO_AUTO || !split_mma_ok(p)) {
             *out = split_mma_ok(p) ? p->algo : CS_ALGO_SPLIT_FMA;
             return CS_OK;
@@ -453,6 +476,9 @@ CS_API cs_status cs_device_wait_timeouts(unsigned *count, int reset)
     unsigned a = 0, b = 0;
     CS_CUDA(cs::split_wait_timeouts(&a, reset != 0));
     CS_CUDA(cs::split_tc_wait_timeouts(&b, reset != 0));
+    unsigned c3 = 0;
+    CS_CUDA(cs::split_tc3d_wait_timeouts(&c3, reset != 0));
+    b += c3;
     *count = a + b;
     return CS_OK;
 }
@@ -535,10 +561,15 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
         if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
+        if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
+            p->algo = (int)v;
+            return CS_OK;
+        }
         if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_MMA_TMA || v == CS_ALGO_SPLIT_TC) &&
             !split_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
-                        "split MMA serves 2D radius-3 plans of at least 8x8 on even-aligned layouts");
+                        "split MMA serves 2D radius-3 plans of at least 8x8 on even-aligned layouts "
+                        "(and tcgen05 also 3D radius-1 plans)");
         p->algo = (int)v;
         return CS_OK;
     case CS_OPT_REANCHOR_INTERVAL:

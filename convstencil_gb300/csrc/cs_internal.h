@@ -72,11 +72,24 @@ cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long
 // 2D tensor map over a whole (hi, lo) buffer of `rows` x `ld` pairs, box_x x box_y tiles.
 cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long long ld, long long rows,
                                     unsigned box_x, unsigned box_y);
+// 3D tensor map: `planes` planes of pitch ldz, rows of pitch ld; box
+// box_x x box_y x 1.
+cudaError_t encode_split_window_map_3d(CUtensorMap *map, const float2 *base, long long ld, long long ldz,
+                                       long long planes, unsigned box_x, unsigned box_y);
+// tcgen05 slice kernel for dense 3x3x3 (27-point) split plans
+// (cs_kernels_split_tc3d.cu). Needs even row and plane pitches, a plane pitch
+// that is a whole number of rows, an even interior column offset and 16-byte
+// aligned buffers.
+bool split_tc3d_layout_ok(const GridView &g, long long origin, const void *in_base, const void *out_base);
+cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
+                                    long long elements, const float2 *in_base, float2 *out_base,
+                                    cudaStream_t stream);
 int device_sm_count();
 // Bounded device-side waits that expired since the last reset (TMA/mma.sync
-// kernel and tcgen05 kernel).
+// kernel, 2D and 3D tcgen05 kernels).
 cudaError_t split_wait_timeouts(unsigned *count, bool reset);
 cudaError_t split_tc_wait_timeouts(unsigned *count, bool reset);
+cudaError_t split_tc3d_wait_timeouts(unsigned *count, bool reset);
 // Whole-buffer conversions and re-anchoring over n elements.
 cudaError_t launch_split_from_fp64(long long n, const double *src, float2 *dst, cudaStream_t stream);
 cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cudaStream_t stream);

@@ -49,6 +49,7 @@
 // TMA copy and the MMAs it still has in flight, frees its TMEM and leaves.
 #include "cs_internal.h"
 #include "cs_split_common.cuh"
+#include "cs_tc_common.cuh"
 
 #include <cuda.h>
 
@@ -66,6 +67,7 @@ using split::kDigits;
 using split::SliceWeights;
 using split::slice_digits;
 using split::two_sum;
+using namespace tc;
 
 // Warp roles.
 constexpr int kSliceWarps = 8, kEpiWarps = 8;
@@ -86,7 +88,6 @@ constexpr int NCOL = NLV * kDigits;        // 160: level L at NLV * L
 constexpr int kAccStride = 256;            // TMEM columns between the two accumulators
 constexpr int kTmemCols = 512;
 constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 40,320
-constexpr unsigned long long kWaitNs = 2000000000ull;
 constexpr int PAIRS = ST_X / 2, NPAIR = ST_Y * PAIRS;           // 36, 2,520
 constexpr int PER = (NPAIR + kSliceThreads - 1) / kSliceThreads;  // 10
 static_assert(kEpiWarps == 2 * 4 && R == 4, "two epilogue warps per TMEM lane quarter, two rows each");
@@ -104,124 +105,6 @@ struct Smem {
     int scale_exp[4];                          // per-tile input scale, ring of 4
     float red[kSliceWarps];
 };
-
-__device__ __forceinline__ unsigned smem_addr(const void *p)
-{
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ unsigned long long globaltimer()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
-{
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Waits for the phase with the given parity. Gives up after kWaitNs (counted
-// in g_tc_wait_timeouts, and *abort raised so every other role stops too) or
-// as soon as another role has raised *abort.
-__device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity, volatile int *abort)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long t0 = globaltimer();
-    for (;;) {
-        for (int i = 0; i < 16; ++i)
-            if (mbar_try_wait(bar, parity)) return true;
-        if (*abort) return false;
-        if (globaltimer() - t0 > kWaitNs) {
-            atomicAdd(&g_tc_wait_timeouts, 1u);
-            *abort = 1;
-            return false;
-        }
-    }
-}
-
-// Unbounded-free wait used only at exit for copies / MMAs still in flight.
-__device__ __noinline__ bool mbar_drain(unsigned bar, unsigned parity)
-{
-    const unsigned long long t0 = globaltimer();
-    while (!mbar_try_wait(bar, parity))
-        if (globaltimer() - t0 > kWaitNs) {
-            atomicAdd(&g_tc_wait_timeouts, 1u);
-            return false;
-        }
-    return true;
-}
-
-__device__ __forceinline__ void mbar_arrive(unsigned bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major, no swizzle; lbo = byte stride of
-// the 16-byte K chunks, sbo = byte stride of the 8-row groups.
-__device__ __forceinline__ unsigned long long smem_desc(unsigned addr, unsigned lbo, unsigned sbo)
-{
-    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)(lbo >> 4) << 16) |
-           ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
-}
-
-// Instruction descriptor of kind::f16: FP16 A and B, FP32 D, both K-major, M = 128.
-__host__ __device__ constexpr unsigned instr_desc(int n)
-{
-    return (1u << 4) | ((unsigned)(n >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_f16(unsigned d_tmem, unsigned long long a, unsigned long long b,
-                                        unsigned idesc, unsigned accumulate)
-{
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(unsigned bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld8(unsigned taddr, float (&v)[8])
-{
-    unsigned r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                   "=r"(r[7])
-                 : "r"(taddr));
-#pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
-}
-
-__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map, int x, int y,
-                                            unsigned bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
-        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
 
 // The MMAs of one tile: window row offset I, input digit D. Descriptor
 // addresses advance in 16-byte units: digit planes are PL halves apart, row
@@ -258,6 +141,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     volatile int *abort = &S.abort;
     const unsigned stage_full = smem_addr(&S.stage_full), stage_empty = smem_addr(&S.stage_empty);
     auto bar2 = [](unsigned long long (&b)[2], int i) { return smem_addr(&b[i]); };
+    auto wait = [abort](unsigned bar, unsigned parity) {
+        return mbar_wait(bar, parity, abort, &g_tc_wait_timeouts);
+    };
 
     int issued = 0, committed = 0;  // window loads issued / MMA batches committed (one thread each)
     if (tid == 0) {
@@ -313,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
             for (int it = issued; it < my_tiles; ++it) {
-                if (!mbar_wait(stage_empty, (it & 1) ^ 1, abort)) break;
+                if (!wait(stage_empty, (it & 1) ^ 1)) break;
                 int x0, y0;
                 tile_origin(it, x0, y0);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -332,8 +218,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             for (int it = 0; it < my_tiles; ++it) {
                 const int buf = it & 1, use = it >> 1;
-                if (!mbar_wait(bar2(S.planes_full, buf), use & 1, abort)) break;
-                if (!mbar_wait(bar2(S.acc_empty, buf), (use & 1) ^ 1, abort)) break;
+                if (!wait(bar2(S.planes_full, buf), use & 1)) break;
+                if (!wait(bar2(S.acc_empty, buf), (use & 1) ^ 1)) break;
                 tc_fence_after();
                 // The issuing thread stalls on every MMA until the tensor core
                 // takes it, so nothing else sits between them: all 50 are
@@ -351,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int it = 0; it < my_tiles; ++it) {
             const int buf = it & 1, use = it >> 1;
             // (a) window landed? One thread waits, the barrier shares the answer.
-            if (leader) S.wait_ok[0] = mbar_wait(stage_full, it & 1, abort);
+            if (leader) S.wait_ok[0] = wait(stage_full, it & 1);
             asm volatile("bar.sync %0, %1;" ::"n"(kSliceBarrier), "n"(kSliceThreads) : "memory");
             if (!S.wait_ok[0]) break;
             // (b) window -> registers, then release the stage to the next load.
@@ -375,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 mbar_arrive(stage_empty);
             }
             // (c) planes of this buffer free (MMAs two tiles back done)?
-            if (leader) S.wait_ok[1] = mbar_wait(bar2(S.planes_empty, buf), (use & 1) ^ 1, abort);
+            if (leader) S.wait_ok[1] = wait(bar2(S.planes_empty, buf), (use & 1) ^ 1);
             asm volatile("bar.sync %0, %1;" ::"n"(kSliceBarrier), "n"(kSliceThreads) : "memory");
             const bool go = S.wait_ok[1];
             vmax = S.red[0];
@@ -414,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const unsigned lane_bits = (unsigned)(32 * quarter) << 16;
         for (int it = 0; it < my_tiles; ++it) {
             const int buf = it & 1, use = it >> 1;
-            if (!mbar_wait(bar2(S.acc_full, buf), use & 1, abort)) break;
+            if (!wait(bar2(S.acc_full, buf), use & 1)) break;
             tc_fence_after();
             int x0, y0;
             tile_origin(it, x0, y0);
@@ -464,9 +350,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     // the shared memory and TMEM are released.
     tc_fence_before();
     __syncthreads();
-    if (warp == kWarpTma && lane == 0 && issued > 0) mbar_drain(stage_full, (issued - 1) & 1);
+    if (warp == kWarpTma && lane == 0 && issued > 0)
+        mbar_drain(stage_full, (issued - 1) & 1, &g_tc_wait_timeouts);
     if (warp == kWarpMma && lane == 0 && committed > 0)
-        mbar_drain(bar2(S.acc_full, (committed - 1) & 1), ((committed - 1) >> 1) & 1);
+        mbar_drain(bar2(S.acc_full, (committed - 1) & 1), ((committed - 1) >> 1) & 1, &g_tc_wait_timeouts);
     __syncthreads();
     tc_fence_after();
     if (warp == kWarpTma)

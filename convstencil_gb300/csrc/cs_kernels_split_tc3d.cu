@@ -1,0 +1,491 @@
+// cs_kernels_split_tc3d.cu — split-precision sweep for dense 3x3x3 (27-point)
+// kernels on the fifth-generation tensor cores (tcgen05.mma, TMEM).
+//
+// Arithmetic: as in the 2D tcgen05 kernel (cs_kernels_split_tc.cu). Inputs
+// (hi, lo) are scaled by a power of two per input plane of a tile and cut
+// into five balanced 9-bit digits held exactly in FP16; the weights are cut
+// the same way with one scale. Products of digit k of x and digit e of w with
+// k + e = L land in one FP32 accumulator per level L, input plane and output
+// plane; such a level sums at most 9 * 5 products below 2^16, so it is exact
+// in any order, and the levels are recombined error-free into (hi, lo).
+//
+// Mapping (M = 128, K = 16):
+//   * A work item is a column of output tiles, 16 rows x 64 columns on zc
+//     consecutive planes. The CTA loads each input plane of the column once
+//     (planes z0-1 .. z0+zc), by one 3D TMA load of rows y0-1 .. y0+16 and
+//     columns x0-4 .. x0+67, and cuts it into five digit planes (18 rows of
+//     72 halves).
+//   * Row m of A is the 16-wide window of block b = m % 8 (8 output columns)
+//     in output row r = m / 8: a K-major, non-swizzled descriptor with a
+//     16-byte K-chunk stride and a stride of one plane row between 8-row
+//     groups reads it out of the digit plane in place; window row offset i
+//     (0..2) is the same descriptor started i rows lower.
+//   * Input plane P feeds output planes P+1, P and P-1 as their z taps
+//     dz = 0, 1, 2, and its MMAs serve all three at once: column n of B_i is
+//     (weight digit e, tap plane dz, column c), n = 32 e + 8 dz + c, with
+//     B[k][n] = w_e[dz][i][k - c - 3] (n with dz = 3 is zero padding that
+//     keeps every level 32 columns wide). For input digit d one MMA with
+//     N = 32 (5 - d) feeds levels d..4 of the plane's TMEM block: 3 row
+//     offsets x 5 digits = 15 MMAs per input plane and 1024 outputs.
+//   * Each input plane has its own 160-column TMEM block (ring of three,
+//     columns 0, 160, 320), so every plane keeps its own scale. Output plane
+//     z reads block z-1 (dz = 0 columns), block z (dz = 1) and block z+1
+//     (dz = 2); block z-1 has then served its last output and is handed back
+//     to the MMA thread as soon as it is read.
+//   * Roles: one warp issues the window loads (two stage buffers), one
+//     thread issues the MMAs, two groups of four warps cut alternate input
+//     planes into digit planes (ring of seven; a plane is too small for
+//     eight warps to share without waiting on each other),
+//     eight warps (a TMEM lane quarter and half of the 8 columns each)
+//     recombine each plane's levels, add the three double-float partial sums
+//     relative to the largest plane scale, scale once and store.
+//
+// Every mbarrier wait is bounded (2 s of %globaltimer). An expired wait is
+// counted in g_tc3d_wait_timeouts; the CTA then waits, again bounded, for the
+// TMA copies and the MMAs it still has in flight, frees its TMEM and leaves.
+#include "cs_internal.h"
+#include "cs_split_common.cuh"
+#include "cs_tc_common.cuh"
+
+#include <algorithm>
+#include <mutex>
+
+namespace cs {
+
+__device__ unsigned int g_tc3d_wait_timeouts;
+
+namespace {
+
+using split::kDigitBits;
+using split::kDigits;
+using split::SliceWeights;
+using split::slice_digits;
+using split::two_sum;
+using namespace tc;
+
+// Warp roles.
+constexpr int kSliceWarps = 8, kEpiWarps = 8;
+constexpr int kWarpTma = 0, kWarpMma = 1, kWarpSlice0 = 2, kWarpEpi0 = kWarpSlice0 + kSliceWarps;
+constexpr int kThreads = 32 * (kWarpEpi0 + kEpiWarps);  // 576
+constexpr int kGroupWarps = kSliceWarps / 2;  // two slicer groups take alternate planes
+constexpr int kGroupThreads = 32 * kGroupWarps;
+constexpr int kSliceBarrier = 1;             // named barriers 1 and 2: one per slicer group
+
+constexpr int G = 16;                        // output rows per tile (M = G x 8 blocks = 128)
+constexpr int TX = 64, TY = G;               // output tile 16 x 64
+constexpr int ST_X = TX + 8, ST_Y = TY + 2;  // window: columns x0-4 .. x0+67, rows y0-1 .. y0+16
+constexpr int PL = ST_X * ST_Y;              // halves per digit plane (2,592 bytes)
+constexpr unsigned kRowBytes = ST_X * 2;     // 144
+constexpr int NOFF = 3;                      // window row offsets
+constexpr int NLV = 32;                      // TMEM columns per level: 4 tap planes (3 + padding) x 8
+constexpr int NCOL = NLV * kDigits;          // 160 columns per input-plane block
+constexpr int NBLK = 3;                      // input-plane blocks in TMEM (ring)
+constexpr int kTmemCols = 512;
+constexpr int kStages = 2;                   // TMA window buffers
+constexpr int NPL = 7;                       // digit-plane sets (ring); also keeps one CTA per SM
+constexpr int kScaleRing = 32;               // per-input-plane scale exponents (ring)
+constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 10,368
+constexpr int PAIRS = ST_X / 2, NPAIR = ST_Y * PAIRS;           // 36, 648
+constexpr int PER = (NPAIR + kGroupThreads - 1) / kGroupThreads;  // 6
+static_assert(NBLK * NCOL <= kTmemCols, "TMEM blocks exceed the allocation");
+static_assert(kEpiWarps == 8, "two epilogue warps per TMEM lane quarter, four columns each");
+static_assert(kStageBytes % 128 == 0, "TMA destinations stay 128-byte aligned");
+
+struct Smem {
+    float2 stage[kStages][ST_Y * ST_X];        // TMA destinations
+    __half planes[NPL][kDigits][PL];           // digit planes of input planes (ring)
+    __half bmat[NOFF][NCOL * 16];              // B_i, K-major 8x16-byte core matrices
+    unsigned long long stage_full[kStages], stage_empty[kStages];
+    unsigned long long planes_full[NPL], planes_empty[NPL];
+    unsigned long long blk_full[NBLK], blk_empty[NBLK];
+    unsigned tmem;                             // TMEM base column
+    int abort;                                 // set by the first expired wait
+    int wait_ok[2][2];                         // slicer group leaders' wait results
+    int scale_exp[kScaleRing];                 // input-plane scale exponents by plane sequence
+    float red[2][kGroupWarps];
+};
+
+// The MMAs of one input plane: window row offset I, input digit D. `a`
+// addresses digit 0, row 0 of the plane's digit planes; descriptor
+// addresses advance in 16-byte units.
+template <int I, int D>
+__device__ __forceinline__ void plane_mma(unsigned d_base, unsigned long long a, unsigned long long b0)
+{
+    constexpr unsigned long long a_off = ((unsigned long long)D * PL * 2 + I * kRowBytes) >> 4;
+    constexpr unsigned long long b_off = ((unsigned long long)I * NCOL * 16 * 2) >> 4;
+    static_assert(((unsigned long long)D * PL * 2 + I * kRowBytes) % 16 == 0 && (NCOL * 16 * 2) % 16 == 0,
+                  "descriptor offsets must be 16-byte multiples");
+    mma_f16(d_base + (unsigned)(NLV * D), a + a_off, b0 + b_off, instr_desc(NLV * (kDigits - D)),
+            (I | D) != 0 ? 1u : 0u);
+    if constexpr (D + 1 < kDigits)
+        plane_mma<I, D + 1>(d_base, a, b0);
+    else if constexpr (I + 1 < NOFF)
+        plane_mma<I + 1, 0>(d_base, a, b0);
+}
+
+// Work item `item` of the sweep: output tile column (x0, y0) on planes
+// zs .. zs + zn - 1. Items run x fastest, then y, then the plane chunk, so
+// CTAs working at the same time share window rows in L2.
+struct Item {
+    int x0, y0, zs, zn;
+};
+
+__device__ __forceinline__ Item item_of(int item, int tiles_x, int tiles_y, int zc, int h)
+{
+    const int txy = tiles_x * tiles_y;
+    const int chunk = item / txy, rem = item - chunk * txy;
+    const int ty = rem / tiles_x;
+    Item it;
+    it.x0 = (rem - ty * tiles_x) * TX;
+    it.y0 = ty * TY;
+    it.zs = chunk * zc;
+    it.zn = min(zc, h - it.zs);
+    return it;
+}
+
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, float (&v)[4])
+{
+    unsigned r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Recombines five exact level sums (level L in units of 2^-9L) into a
+// double-float pair.
+__device__ __forceinline__ void recombine(const float (&acc)[kDigits], float &hi, float &lo)
+{
+    float h1, e1, h2, e2;
+    two_sum(acc[0], acc[1] * 0x1p-9f, h1, e1);
+    two_sum(h1, acc[2] * 0x1p-18f, h2, e2);
+    const float tail = fmaf(acc[3], 0x1p-27f, acc[4] * 0x1p-36f);
+    two_sum(h2, (e1 + e2) + tail, hi, lo);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k3d_tc(const __grid_constant__ CUtensorMap tmap, float2 *__restrict__ out, int h, int m, int n,
+           long long ldy, long long ldz, int tiles_x, int tiles_y, int zc, int items, int map_x, int map_y,
+           int map_z, SliceWeights sw)
+{
+    extern __shared__ unsigned char smem_raw[];
+    Smem &S = *reinterpret_cast<Smem *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    volatile int *abort = &S.abort;
+    auto bar = [](unsigned long long *b, int i) { return smem_addr(&b[i]); };
+    auto wait = [abort](unsigned b, unsigned parity) {
+        return mbar_wait(b, parity, abort, &g_tc3d_wait_timeouts);
+    };
+    const int first = blockIdx.x, step = gridDim.x;
+
+    int issued = 0, committed = 0;  // window loads issued / input planes committed (one thread each)
+    if (tid == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            mbar_init(bar(S.stage_full, i), 1);
+            mbar_init(bar(S.stage_empty, i), kGroupWarps);
+        }
+        for (int i = 0; i < NPL; ++i) {
+            mbar_init(bar(S.planes_full, i), kGroupWarps);
+            mbar_init(bar(S.planes_empty, i), 1);
+        }
+        for (int i = 0; i < NBLK; ++i) {
+            mbar_init(bar(S.blk_full, i), 1);
+            mbar_init(bar(S.blk_empty, i), kEpiWarps);
+        }
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == kWarpTma) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_addr(&S.tmem)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    // B_i: N row nn = NLV e + 8 dz + c (digit e of w, z tap dz, column c of
+    // the block; dz = 3 is padding), K index k.
+    for (int idx = tid; idx < NOFF * NCOL * 16; idx += kThreads) {
+        const int i = idx / (NCOL * 16), rem = idx - i * (NCOL * 16);
+        const int nn = rem >> 4, k = rem & 15;
+        const int e = nn / NLV, dz = (nn % NLV) >> 3, c = nn & 7;
+        const int tj = k - c - 3;
+        const __half v = (dz < 3 && tj >= 0 && tj < 3) ? sw.d[e][(dz * 3 + i) * 3 + tj] : __float2half(0.f);
+        S.bmat[i][(nn >> 3) * 128 + (nn & 7) * 8 + (k >> 3) * 64 + (k & 7)] = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = S.tmem;
+
+    if (warp == kWarpTma) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            int q = 0;  // input-plane sequence number
+            bool ok = true;
+            for (int item = first; item < items && ok; item += step) {
+                const Item w = item_of(item, tiles_x, tiles_y, zc, h);
+                for (int p = 0; p < w.zn + 2; ++p, ++q) {
+                    const int sb = q & 1;
+                    if (!(ok = wait(bar(S.stage_empty, sb), ((q >> 1) & 1) ^ 1))) break;
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_expect_tx(bar(S.stage_full, sb), kStageBytes);
+                    tma_load_3d(smem_addr(S.stage[sb]), &tmap, map_x + w.x0 - 4, map_y + w.y0 - 1,
+                                map_z + w.zs - 1 + p, bar(S.stage_full, sb));
+                    issued = q + 1;
+                }
+            }
+        }
+    } else if (warp == kWarpMma) {
+        // ------------------------------------------------ MMA issuer
+        const unsigned long long a_desc0 = smem_desc(smem_addr(S.planes[0][0]), 16, kRowBytes);
+        constexpr unsigned long long kSetUnits = (unsigned long long)kDigits * PL * 2 / 16;
+        const unsigned long long b_desc0 = smem_desc(smem_addr(S.bmat[0]), 128, 256);
+        if (lane == 0) {
+            int q = 0;
+            bool ok = true;
+            for (int item = first; item < items && ok; item += step) {
+                const Item w = item_of(item, tiles_x, tiles_y, zc, h);
+                for (int p = 0; p < w.zn + 2; ++p, ++q) {
+                    const int slot = q % NPL, blk = q % NBLK;
+                    if (!(ok = wait(bar(S.planes_full, slot), (q / NPL) & 1) &&
+                               wait(bar(S.blk_empty, blk), ((q / NBLK) & 1) ^ 1)))
+                        break;
+                    tc_fence_after();
+                    plane_mma<0, 0>(tmem + (unsigned)(NCOL * blk), a_desc0 + kSetUnits * slot, b_desc0);
+                    mma_commit(bar(S.blk_full, blk));       // block ready for the epilogue
+                    mma_commit(bar(S.planes_empty, slot));  // digit planes may be overwritten
+                    committed = q + 1;
+                }
+            }
+        }
+    } else if (warp < kWarpEpi0) {
+        // ------------------------------------------------ slicers
+        // Group grp (four warps) cuts the planes with q % 2 == grp, from
+        // stage buffer grp; the two groups work on consecutive planes at the
+        // same time.
+        const int grp = (warp - kWarpSlice0) / kGroupWarps, gw = (warp - kWarpSlice0) % kGroupWarps;
+        const int st = tid - 32 * (kWarpSlice0 + kGroupWarps * grp);
+        const bool leader = st == 0;
+        int q = 0;
+        bool go = true;
+        for (int item = first; item < items && go; item += step) {
+            const Item w = item_of(item, tiles_x, tiles_y, zc, h);
+            for (int p = 0; p < w.zn + 2; ++p, ++q) {
+                if ((q & 1) != grp) continue;
+                const int sb = q & 1, slot = q % NPL;
+                // (a) window landed? One thread waits, the barrier shares the answer.
+                if (leader) S.wait_ok[grp][0] = wait(bar(S.stage_full, sb), (q >> 1) & 1);
+                asm volatile("bar.sync %0, %1;" ::"r"(kSliceBarrier + grp), "n"(kGroupThreads) : "memory");
+                if (!S.wait_ok[grp][0]) {
+                    go = false;
+                    break;
+                }
+                // (b) window -> registers, then release the stage to the next load.
+                const float4 *stg = reinterpret_cast<const float4 *>(S.stage[sb]);
+                float4 v[PER];
+                float vmax = 0.f;
+#pragma unroll
+                for (int k = 0; k < PER; ++k) {
+                    const int idx = st + k * kGroupThreads;
+                    v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (idx < NPAIR) {
+                        v[k] = stg[idx];
+                        vmax = fmaxf(vmax, fmaxf(fabsf(v[k].x), fabsf(v[k].z)));
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+                __syncwarp();
+                if (lane == 0) {
+                    S.red[grp][gw] = vmax;
+                    mbar_arrive(bar(S.stage_empty, sb));
+                }
+                // (c) digit-plane set free (the MMAs that read it are done)?
+                if (leader) S.wait_ok[grp][1] = wait(bar(S.planes_empty, slot), ((q / NPL) & 1) ^ 1);
+                asm volatile("bar.sync %0, %1;" ::"r"(kSliceBarrier + grp), "n"(kGroupThreads) : "memory");
+                go = S.wait_ok[grp][1];
+                vmax = S.red[grp][0];
+#pragma unroll
+                for (int i = 1; i < kGroupWarps; ++i) vmax = fmaxf(vmax, S.red[grp][i]);
+                // (d) every slicer of the group has read wait_ok and red before they are reused
+                asm volatile("bar.sync %0, %1;" ::"r"(kSliceBarrier + grp), "n"(kGroupThreads) : "memory");
+                if (!go) break;
+                const int ex = split::tile_exponent(vmax);
+                if (leader) S.scale_exp[q % kScaleRing] = ex;
+                const float to_digits = ldexpf(1.0f, kDigitBits - ex);
+#pragma unroll
+                for (int k = 0; k < PER; ++k) {
+                    const int idx = st + k * kGroupThreads;
+                    if (idx < NPAIR) {
+                        float d0[kDigits], d1[kDigits];
+                        slice_digits(v[k].x * to_digits, v[k].y * to_digits, d0);
+                        slice_digits(v[k].z * to_digits, v[k].w * to_digits, d1);
+                        unsigned *dst = reinterpret_cast<unsigned *>(&S.planes[slot][0][0]) + idx;
+#pragma unroll
+                        for (int dg = 0; dg < kDigits; ++dg)
+                            dst[dg * (PL / 2)] = split::pack_h2(d0[dg], d1[dg]);
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(S.planes_full, slot));
+            }
+        }
+    } else {
+        // ------------------------------------------------ epilogue
+        // Warp w reads TMEM lanes 32 (w % 4) ..; lane -> D row m = (output
+        // row er, block eb); warp half hh takes columns 8 eb + 4 hh .. + 3.
+        const int quarter = warp & 3, hh = (warp - kWarpEpi0) >> 2;
+        const int mrow = 32 * quarter + lane;
+        const int er = mrow >> 3, eb = mrow & 7;
+        const unsigned lane_bits = (unsigned)(32 * quarter) << 16;
+        int q0 = 0;  // first input plane of the item
+        bool ok = true;
+        for (int item = first; item < items && ok; item += step) {
+            const Item w = item_of(item, tiles_x, tiles_y, zc, h);
+            const int xb = w.x0 + 8 * eb + 4 * hh, yy = w.y0 + er;
+            for (int j = 0; j < w.zn; ++j) {
+                // Blocks of input planes q0+j .. q0+j+2; the first two of an
+                // item were not waited for by an earlier output.
+                for (int q = (j == 0 ? q0 : q0 + j + 2); q <= q0 + j + 2 && ok; ++q)
+                    ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1);
+                if (!ok) break;
+                tc_fence_after();
+                // Partial sums are added relative to the largest input-plane
+                // scale (exact powers of two), and scaled to absolute values
+                // once at the end, so near the bottom of FP32's range only the
+                // final product rounds into subnormals.
+                int exd[3];
+#pragma unroll
+                for (int dz = 0; dz < 3; ++dz) exd[dz] = S.scale_exp[(q0 + j + dz) % kScaleRing];
+                const int exm = max(exd[0], max(exd[1], exd[2]));
+                float sh[4], sl[4];
+#pragma unroll
+                for (int dz = 0; dz < 3; ++dz) {
+                    const int qq = q0 + j + dz;
+                    const unsigned col = (unsigned)(NCOL * (qq % NBLK) + 8 * dz + 4 * hh);
+                    float acc[kDigits][4];
+#pragma unroll
+                    for (int L = 0; L < kDigits; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
+                    tmem_wait_ld();
+                    // Block qq served its last output: it is the z-1 plane
+                    // here, or one of the last planes of the column.
+                    if (dz == 0 || j == w.zn - 1) {
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(bar(S.blk_empty, qq % NBLK));
+                    }
+                    const float rel = ldexpf(1.0f, exd[dz] - exm);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        float lv[kDigits], hi, lo;
+#pragma unroll
+                        for (int L = 0; L < kDigits; ++L) lv[L] = acc[L][c];
+                        recombine(lv, hi, lo);
+                        hi *= rel;
+                        lo *= rel;
+                        if (dz == 0) {
+                            sh[c] = hi;
+                            sl[c] = lo;
+                        } else {
+                            float s, e;
+                            two_sum(sh[c], hi, s, e);
+                            sh[c] = s;
+                            sl[c] += e + lo;
+                        }
+                    }
+                }
+                if (yy < m) {
+                    const float scale = ldexpf(1.0f, exm + sw.ew - 2 * kDigitBits);
+                    float2 res[4];
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        float hi, lo;
+                        two_sum(sh[c], sl[c], hi, lo);
+                        res[c] = make_float2(hi * scale, lo * scale);
+                    }
+                    float2 *op = out + (long long)(w.zs + j) * ldz + (long long)yy * ldy + xb;
+#pragma unroll
+                    for (int c = 0; c < 4; c += 2) {
+                        if (xb + c + 1 < n)
+                            *reinterpret_cast<float4 *>(op + c) =
+                                make_float4(res[c].x, res[c].y, res[c + 1].x, res[c + 1].y);
+                        else if (xb + c < n)
+                            op[c] = res[c];
+                    }
+                }
+            }
+            q0 += w.zn + 2;
+        }
+    }
+
+    // Exit: every role is done or has given up. Let the last window loads and
+    // the last MMA batch finish (they have normally finished already) before
+    // the shared memory and TMEM are released.
+    tc_fence_before();
+    __syncthreads();
+    if (warp == kWarpTma && lane == 0)
+        for (int l = max(0, issued - kStages); l < issued; ++l)
+            mbar_drain(bar(S.stage_full, l & 1), (l >> 1) & 1, &g_tc3d_wait_timeouts);
+    if (warp == kWarpMma && lane == 0 && committed > 0)
+        mbar_drain(bar(S.blk_full, (committed - 1) % NBLK), ((committed - 1) / NBLK) & 1,
+                   &g_tc3d_wait_timeouts);
+    __syncthreads();
+    tc_fence_after();
+    if (warp == kWarpTma)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+}  // namespace
+
+bool split_tc3d_layout_ok(const GridView &g, long long origin, const void *in_base, const void *out_base)
+{
+    if (g.dims != 3) return false;
+    const long long ldy = g.pitch[1], ldz = g.pitch[0];
+    return ldy % 2 == 0 && ldz % 2 == 0 && ldz % ldy == 0 && (origin % ldy) % 2 == 0 &&
+           reinterpret_cast<uintptr_t>(in_base) % 16 == 0 && reinterpret_cast<uintptr_t>(out_base) % 16 == 0;
+}
+
+cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
+                                    long long elements, const float2 *in_base, float2 *out_base,
+                                    cudaStream_t st)
+{
+    const long long ldy = g.pitch[1], ldz = g.pitch[0];
+    CUtensorMap map;
+    cudaError_t e = encode_split_window_map_3d(&map, in_base, ldy, ldz, elements / ldz, ST_X, ST_Y);
+    if (e != cudaSuccess) return e;
+    const size_t smem = sizeof(Smem) + 128;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [smem] {
+        attr_err = cudaFuncSetAttribute(k3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    if (attr_err != cudaSuccess) return attr_err;
+    const int h = (int)g.ext[0], m = (int)g.ext[1], n = (int)g.ext[2];
+    const int tiles_x = (n + TX - 1) / TX, tiles_y = (m + TY - 1) / TY;
+    // Planes per work item: up to 32 (each column re-reads two planes), fewer
+    // when that would leave SMs without several items.
+    const int sms = device_sm_count();
+    const long long txy = (long long)tiles_x * tiles_y;
+    const long long want = 8LL * sms;
+    const int zc = (int)std::max(1LL, std::min(32LL, (h * txy + want - 1) / want));
+    const int items = (int)(txy * ((h + zc - 1) / zc));
+    const int grid = std::min(items, sms);
+    note_launch();
+    k3d_tc<<<grid, kThreads, smem, st>>>(map, out_base + origin, h, m, n, ldy, ldz, tiles_x, tiles_y, zc,
+                                        items, (int)(origin % ldy), (int)((origin % ldz) / ldy),
+                                        (int)(origin / ldz), split::slice_weights(w, 27));
+    return cudaGetLastError();
+}
+
+cudaError_t split_tc3d_wait_timeouts(unsigned *count, bool reset)
+{
+    cudaError_t e = cudaMemcpyFromSymbol(count, g_tc3d_wait_timeouts, sizeof(unsigned));
+    if (e != cudaSuccess || !reset) return e;
+    const unsigned zero = 0;
+    return cudaMemcpyToSymbol(g_tc3d_wait_timeouts, &zero, sizeof(unsigned));
+}
+
+}  // namespace cs

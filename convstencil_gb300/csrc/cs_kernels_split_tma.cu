@@ -327,6 +327,23 @@ cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long l
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// 3D form: planes of `rows` rows of pitch ld, plane pitch ldz; box
+// box_x x box_y x 1.
+cudaError_t encode_split_window_map_3d(CUtensorMap *map, const float2 *base, long long ld, long long ldz,
+                                       long long planes, unsigned box_x, unsigned box_y)
+{
+    auto encode = encode_fn();
+    if (!encode) return cudaErrorNotSupported;
+    cuuint64_t dims[3] = {(cuuint64_t)ld, (cuuint64_t)(ldz / ld), (cuuint64_t)planes};
+    cuuint64_t strides[2] = {(cuuint64_t)(ld * sizeof(float2)), (cuuint64_t)(ldz * sizeof(float2))};
+    cuuint32_t box[3] = {box_x, box_y, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2 *>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 bool split_tma_layout_ok(const GridView &g, long long origin, const void *base)
 {
     if (g.dims != 2) return false;

@@ -58,7 +58,7 @@ constexpr int kDigitBits = 9;    // balanced base-512 digits, |d| <= 256
 constexpr float kRadix = 512.f;
 
 struct SliceWeights {
-    __half d[kDigits][49];  // digits of w / 2^Ew, row-major 7x7
+    __half d[kDigits][49];  // digits of w / 2^Ew: row-major 7x7, or 3x3x3 in the first 27
     int ew;                 // weight scale exponent: |w| < 2^(ew-1)
 };
 
@@ -122,18 +122,19 @@ constexpr int SL_PLANE = SL_Y * SL_PITCH;
 
 // Balanced base-512 digits of w / 2^ew for the 49 taps (exact in double);
 // ew is chosen so that every |w| / 2^ew < 1/2.
-inline SliceWeights slice_weights(const Weights &w)
+// The first `taps` weights (49: a 7x7 kernel; 27: a 3x3x3 kernel), one scale.
+inline SliceWeights slice_weights(const Weights &w, int taps = 49)
 {
     SliceWeights s{};
     double mx = 0.0;
-    for (int i = 0; i < 49; ++i) mx = std::fmax(mx, std::fabs(w.v[i]));
+    for (int i = 0; i < taps; ++i) mx = std::fmax(mx, std::fabs(w.v[i]));
     int e = 0;
     if (mx > 0.0) {
         std::frexp(mx, &e);  // mx < 2^e
         e += 1;
     }
     s.ew = e;
-    for (int i = 0; i < 49; ++i) {
+    for (int i = 0; i < taps; ++i) {
         double a = std::ldexp(w.v[i], kDigitBits - e);
         for (int k = 0; k < kDigits; ++k) {  // balanced digits, |d| <= 256
             const double d = std::rint(a);

@@ -205,6 +205,64 @@ def test_split_buffers_offset_by_one_pair(algo):
     assert rel_err(p.unpack(out.cpu().numpy()), p.unpack(ref))[0] <= TOL
 
 
+@pytest.mark.parametrize("ext", [(17, 35, 40), (70, 33, 65), (40, 96, 130), (1, 40, 70), (1, 1, 1),
+                                 (200, 64, 64)])
+def test_split_tc3d_vs_oracle(ext):
+    """The tcgen05 3D kernel (27 weights): one or many planes per work item,
+    ragged tiles in x and y, inputs of both signs; against the oracle, and
+    bitwise repeatable. (Signed weights: test_split_tc3d_wide_range.)"""
+    rng = np.random.default_rng(sum(ext))
+    w = O.seeded_weights(27, sum(ext))
+    p = cs.Plan("box3d1r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    x = rng.uniform(-1.0, 1.0, ext)
+    buf = p.pack(x)
+    cs.device_wait_timeouts(reset=True)
+    got = split_run(p, buf, 4)
+    again = split_run(p, buf, 4)
+    assert cs.device_wait_timeouts(reset=True) == 0
+    np.testing.assert_array_equal(got, again)
+    ref = oracle_run(p, buf, w, 1, 4)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
+def test_split_tc3d_wide_range():
+    """Signed weights and inputs spanning 40 binades inside each tile: the
+    split digits are relative to the largest weight and to each input plane's
+    largest value in the tile, so the bar is normwise, as for the 2D
+    tensor-core kernels."""
+    ext = (17, 35, 40)
+    rng = np.random.default_rng(7)
+    w = rng.uniform(-1.0, 1.0, 27)
+    w /= np.abs(w).sum()
+    p = cs.Plan("box3d1r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    x = rng.uniform(-1.0, 1.0, ext) * np.exp2(rng.integers(-20, 20, ext))
+    buf = p.pack(x)
+    got = split_run(p, buf, 4)
+    ref = oracle_run(p, buf, w, 1, 4)
+    assert rel_err(p.unpack(got), p.unpack(ref))[1] <= TOL
+
+
+@pytest.mark.parametrize("scale,tol", [(2.0 ** -125, 1e-6), (2.0 ** 100, TOL)])
+def test_split_tc3d_extreme_magnitudes(scale, tol):
+    """3D tcgen05 kernel on grids near the bottom or top of FP32's range,
+    against the FP64 path (the (hi, lo) format keeps ~24 bits near 2^-125)."""
+    ext = (9, 40, 70)
+    w = O.seeded_weights(27, 95)
+    x = O.splitmix_uniform(int(np.prod(ext)), 96).reshape(ext) * scale
+    p64 = cs.Plan("box3d1r", ext, w)
+    buf = p64.pack(x)
+    a = torch.from_numpy(buf).cuda()
+    b = torch.zeros_like(a)
+    ref = (b if p64.run(a, b, 3) else a).cpu().numpy()
+    p = cs.Plan("box3d1r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    got = split_run(p, buf, 3)
+    assert np.isfinite(got).all()
+    assert rel_err(p.unpack(got), p64.unpack(ref))[0] <= tol
+
+
 @pytest.mark.parametrize("ext", [(70, 9, 33), (40, 130, 70), (160, 256, 256), (3, 17, 31), (1, 1, 1)])
 def test_split_star3d_z_marching(ext):
     """The 7-point star's z-marching kernel: one plane per CTA (tall, thin
