@@ -32,7 +32,7 @@
 //     z reads block z-1 (dz = 0 columns), block z (dz = 1) and block z+1
 //     (dz = 2); block z-1 has then served its last output and is handed back
 //     to the MMA thread as soon as it is read.
-//   * Roles: one warp issues the window loads (two stage buffers), one
+//   * Roles: one warp issues the window loads (four stage buffers), one
 //     thread issues the MMAs, two groups of four warps cut alternate input
 //     planes into digit planes (ring of seven; a plane is too small for
 //     eight warps to share without waiting on each other),
@@ -81,7 +81,7 @@ constexpr int NLV = 32;                      // TMEM columns per level: 4 tap pl
 constexpr int NCOL = NLV * kDigits;          // 160 columns per input-plane block
 constexpr int NBLK = 3;                      // input-plane blocks in TMEM (ring)
 constexpr int kTmemCols = 512;
-constexpr int kStages = 2;                   // TMA window buffers
+constexpr int kStages = 4;                   // TMA window buffers (two per slicer group)
 constexpr int NPL = 7;                       // digit-plane sets (ring); also keeps one CTA per SM
 constexpr int kScaleRing = 32;               // per-input-plane scale exponents (ring)
 constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 10,368
@@ -227,8 +227,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int item = first; item < items && ok; item += step) {
                 const Item w = item_of(item, tiles_x, tiles_y, zc, h);
                 for (int p = 0; p < w.zn + 2; ++p, ++q) {
-                    const int sb = q & 1;
-                    if (!(ok = wait(bar(S.stage_empty, sb), ((q >> 1) & 1) ^ 1))) break;
+                    const int sb = q % kStages;
+                    if (!(ok = wait(bar(S.stage_empty, sb), ((q / kStages) & 1) ^ 1))) break;
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(bar(S.stage_full, sb), kStageBytes);
                     tma_load_3d(smem_addr(S.stage[sb]), &tmap, map_x + w.x0 - 4, map_y + w.y0 - 1,
@@ -263,8 +263,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (warp < kWarpEpi0) {
         // ------------------------------------------------ slicers
         // Group grp (four warps) cuts the planes with q % 2 == grp, from
-        // stage buffer grp; the two groups work on consecutive planes at the
-        // same time.
+        // stage buffers grp and grp + 2; the two groups work on consecutive
+        // planes at the same time.
         const int grp = (warp - kWarpSlice0) / kGroupWarps, gw = (warp - kWarpSlice0) % kGroupWarps;
         const int st = tid - 32 * (kWarpSlice0 + kGroupWarps * grp);
         const bool leader = st == 0;
@@ -274,9 +274,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             const Item w = item_of(item, tiles_x, tiles_y, zc, h);
             for (int p = 0; p < w.zn + 2; ++p, ++q) {
                 if ((q & 1) != grp) continue;
-                const int sb = q & 1, slot = q % NPL;
+                const int sb = q % kStages, slot = q % NPL;
                 // (a) window landed? One thread waits, the barrier shares the answer.
-                if (leader) S.wait_ok[grp][0] = wait(bar(S.stage_full, sb), (q >> 1) & 1);
+                if (leader) S.wait_ok[grp][0] = wait(bar(S.stage_full, sb), (q / kStages) & 1);
                 asm volatile("bar.sync %0, %1;" ::"r"(kSliceBarrier + grp), "n"(kGroupThreads) : "memory");
                 if (!S.wait_ok[grp][0]) {
                     go = false;
@@ -347,24 +347,25 @@ __global__ void __launch_bounds__(kThreads, 1)
             const Item w = item_of(item, tiles_x, tiles_y, zc, h);
             const int xb = w.x0 + 8 * eb + 4 * hh, yy = w.y0 + er;
             for (int j = 0; j < w.zn; ++j) {
-                // Blocks of input planes q0+j .. q0+j+2; the first two of an
-                // item were not waited for by an earlier output.
-                for (int q = (j == 0 ? q0 : q0 + j + 2); q <= q0 + j + 2 && ok; ++q)
+                // Blocks of input planes q0+j, q0+j+1 (z taps 0 and 1) were
+                // waited for by the previous output, except at the start of
+                // the column; block q0+j+2 is waited for only after block
+                // q0+j has been read and handed back, so the MMAs of the next
+                // plane never wait for this output's last block.
+                for (int q = q0; j == 0 && q <= q0 + 1 && ok; ++q)
                     ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1);
                 if (!ok) break;
                 tc_fence_after();
-                // Partial sums are added relative to the largest input-plane
-                // scale (exact powers of two), and scaled to absolute values
-                // once at the end, so near the bottom of FP32's range only the
-                // final product rounds into subnormals.
+                float ph[3][4], pl[3][4];  // each tap plane's recombined (hi, lo)
                 int exd[3];
-#pragma unroll
-                for (int dz = 0; dz < 3; ++dz) exd[dz] = S.scale_exp[(q0 + j + dz) % kScaleRing];
-                const int exm = max(exd[0], max(exd[1], exd[2]));
-                float sh[4], sl[4];
 #pragma unroll
                 for (int dz = 0; dz < 3; ++dz) {
                     const int qq = q0 + j + dz;
+                    if (dz == 2) {
+                        if (!(ok = wait(bar(S.blk_full, qq % NBLK), (qq / NBLK) & 1))) break;
+                        tc_fence_after();
+                    }
+                    exd[dz] = S.scale_exp[qq % kScaleRing];
                     const unsigned col = (unsigned)(NCOL * (qq % NBLK) + 8 * dz + 4 * hh);
                     float acc[kDigits][4];
 #pragma unroll
@@ -377,23 +378,35 @@ __global__ void __launch_bounds__(kThreads, 1)
                         __syncwarp();
                         if (lane == 0) mbar_arrive(bar(S.blk_empty, qq % NBLK));
                     }
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        float lv[kDigits];
+#pragma unroll
+                        for (int L = 0; L < kDigits; ++L) lv[L] = acc[L][c];
+                        recombine(lv, ph[dz][c], pl[dz][c]);
+                    }
+                }
+                if (!ok) break;
+                // Partial sums are added relative to the largest input-plane
+                // scale (exact powers of two), and scaled to absolute values
+                // once at the end, so near the bottom of FP32's range only the
+                // final product rounds into subnormals.
+                const int exm = max(exd[0], max(exd[1], exd[2]));
+                float sh[4], sl[4];
+#pragma unroll
+                for (int dz = 0; dz < 3; ++dz) {
                     const float rel = ldexpf(1.0f, exd[dz] - exm);
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        float lv[kDigits], hi, lo;
-#pragma unroll
-                        for (int L = 0; L < kDigits; ++L) lv[L] = acc[L][c];
-                        recombine(lv, hi, lo);
-                        hi *= rel;
-                        lo *= rel;
+                        const float hi = ph[dz][c] * rel, lo = pl[dz][c] * rel;
                         if (dz == 0) {
                             sh[c] = hi;
                             sl[c] = lo;
                         } else {
-                            float s, e;
-                            two_sum(sh[c], hi, s, e);
-                            sh[c] = s;
-                            sl[c] += e + lo;
+                            float s2, e2;
+                            two_sum(sh[c], hi, s2, e2);
+                            sh[c] = s2;
+                            sl[c] += e2 + lo;
                         }
                     }
                 }
@@ -428,7 +441,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     if (warp == kWarpTma && lane == 0)
         for (int l = max(0, issued - kStages); l < issued; ++l)
-            mbar_drain(bar(S.stage_full, l & 1), (l >> 1) & 1, &g_tc3d_wait_timeouts);
+            mbar_drain(bar(S.stage_full, l % kStages), (l / kStages) & 1, &g_tc3d_wait_timeouts);
     if (warp == kWarpMma && lane == 0 && committed > 0)
         mbar_drain(bar(S.blk_full, (committed - 1) % NBLK), ((committed - 1) / NBLK) & 1,
                    &g_tc3d_wait_timeouts);
