@@ -478,12 +478,18 @@ cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long lo
     if (attr_err != cudaSuccess) return attr_err;
     const int h = (int)g.ext[0], m = (int)g.ext[1], n = (int)g.ext[2];
     const int tiles_x = (n + TX - 1) / TX, tiles_y = (m + TY - 1) / TY;
-    // Planes per work item: up to 32 (each column re-reads two planes), fewer
-    // when that would leave SMs without several items.
+    // Planes per work item: a column of zc output planes loads and cuts
+    // zc + 2 input planes, and the busiest CTA takes ceil(items / SMs) items,
+    // so zc (up to 32) minimises ceil(items / SMs) * (zc + 2).
     const int sms = device_sm_count();
     const long long txy = (long long)tiles_x * tiles_y;
-    const long long want = 8LL * sms;
-    const int zc = (int)std::max(1LL, std::min(32LL, (h * txy + want - 1) / want));
+    int zc = 1;
+    long long best = -1;
+    for (int c = 1; c <= std::min(32, h); ++c) {
+        const long long it = txy * ((h + c - 1) / c);
+        const long long cost = ((it + sms - 1) / sms) * (c + 2);
+        if (best < 0 || cost < best) best = cost, zc = c;
+    }
     const int items = (int)(txy * ((h + zc - 1) / zc));
     const int grid = std::min(items, sms);
     note_launch();

@@ -445,11 +445,22 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
     // use), else the double-float kernels with a fixed temporal block (their
     // results do not depend on it).
     if (d->precision == CS_PREC_SPLIT) {
-        // tcgen05 pays a fixed ~16 us per sweep (one 64 x 64 tile per CTA and
-        // SM, set-up of its weight matrices and TMEM); below about four tiles
-        // per SM the mma.sync slice kernel (~8 us floor) finishes sooner.
-        const long long tiles = ((d->extent[0] + 63) / 64) * ((d->extent[1] + 63) / 64);
-        const int algo = tiles >= 4LL * s->sm_count ? CS_ALGO_SPLIT_TC : CS_ALGO_SPLIT_MMA;
+        int algo;
+        if (d->shape == CS_SHAPE_STAR3D1R || d->shape == CS_SHAPE_BOX3D1R) {
+            // 3D: the 27-point box on tcgen05 from about 128^3 points up
+            // (measured crossover), else the double-float kernels (the
+            // 7-point star always: its own kernel is faster).
+            const double pts = (double)d->extent[0] * (double)d->extent[1] * (double)d->extent[2];
+            algo = d->shape == CS_SHAPE_BOX3D1R && d->semantics == CS_SEM_STEP && pts >= 2.0e6
+                       ? CS_ALGO_SPLIT_TC
+                       : CS_ALGO_SPLIT_FMA;
+        } else {
+            // tcgen05 pays a fixed ~16 us per sweep (one 64 x 64 tile per CTA
+            // and SM, set-up of its weight matrices and TMEM); below about four
+            // tiles per SM the mma.sync slice kernel (~8 us floor) finishes sooner.
+            const long long tiles = ((d->extent[0] + 63) / 64) * ((d->extent[1] + 63) / 64);
+            algo = tiles >= 4LL * s->sm_count ? CS_ALGO_SPLIT_TC : CS_ALGO_SPLIT_MMA;
+        }
         if (cs_plan_set_option(r->plan, CS_OPT_ALGO, algo) != CS_OK)
             cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_SPLIT_FMA);
         const int tb = (d->shape == CS_SHAPE_1D1R || d->shape == CS_SHAPE_1D2R) ? 4
