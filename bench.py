@@ -373,18 +373,23 @@ def run_pipe_peaks():
 
 # ------------------------------------------------------------ ncu cases
 def run_kernel_case(args):
-    """One box2d3r plan, one algorithm, `sweeps` sweeps on an m x n grid."""
+    """One box2d3r plan (box3d1r on an h x m x n grid for split_tc3d), one
+    algorithm, `sweeps` sweeps on an m x n grid."""
     import torch
     import convstencil_gb300 as cs
     from oracle import cs_oracle as O
     m, n = args.m, args.n
-    x = O.splitmix_uniform(m * n, GRID_SEED).reshape(m, n)
-    w = O.seeded_weights(TAPS, WEIGHT_SEED)
+    shape, ext, taps = SHAPE, (m, n), TAPS
+    if args.kernel_case == "split_tc3d":
+        shape, ext, taps = "box3d1r", (args.h, m, n), 27
+    x = O.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
+    w = O.seeded_weights(taps, WEIGHT_SEED)
     algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA,
             "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
-            "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC}[args.kernel_case]
+            "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC,
+            "split_tc3d": cs.Algo.SPLIT_TC}[args.kernel_case]
     split = args.kernel_case.startswith("split")
-    p = cs.Plan(SHAPE, (m, n), w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
+    p = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
     p.set_option(cs.Option.ALGO, algo)
     host = torch.from_numpy(p.pack(x)).cuda()
     if split:
@@ -400,8 +405,8 @@ def run_kernel_case(args):
     ev1.record()
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1) / max(1, args.sweeps)
-    print(json.dumps({"kernel_case": args.kernel_case, "m": m, "n": n, "sweeps": args.sweeps,
-                      "ms_per_sweep": round(ms, 4), "gstencil_s": round(m * n / ms / 1e6, 3)}))
+    print(json.dumps({"kernel_case": args.kernel_case, "extent": list(ext), "sweeps": args.sweeps,
+                      "ms_per_sweep": round(ms, 4), "gstencil_s": round(float(np.prod(ext)) / ms / 1e6, 3)}))
     return 0
 
 
@@ -476,11 +481,13 @@ def main():
                     help="requests in the served-stream sample (0 = skip)")
     ap.add_argument("--served-rate", type=float, default=40.0, help="Poisson arrival rate (req/s)")
     ap.add_argument("--kernel-case", default=None,
-                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_mma_tma", "split_fma", "split_tc"],
-                    help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid "
-                         "(small cases for ncu captures) and exit")
+                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_mma_tma", "split_fma", "split_tc",
+                             "split_tc3d"],
+                    help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid (split_tc3d: "
+                         "box3d1r on --h x --m x --n) (small cases for ncu captures) and exit")
     ap.add_argument("--m", type=int, default=4608)
     ap.add_argument("--n", type=int, default=4608)
+    ap.add_argument("--h", type=int, default=256)
     ap.add_argument("--sweeps", type=int, default=4)
     ap.add_argument("--configs", action="store_true",
                     help="measure every BASELINE configuration (FP64, split, reference kernels) and exit")
