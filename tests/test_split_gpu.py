@@ -226,6 +226,27 @@ def test_split_tc3d_vs_oracle(ext):
     assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
 
 
+@pytest.mark.parametrize("ref_layout", [False, True])
+def test_split_tc3d_layouts(ref_layout):
+    """SPLIT_TC pinned on a 3D plan in the reference's layout (interior
+    column 3: the window load could not start 16-byte aligned) falls back to
+    the double-float kernel; in the native layout it runs on tcgen05. Both
+    against the oracle."""
+    from tests.util import layout_3d_ref
+    ext = (12, 37, 70)
+    w = O.seeded_weights(27, 97)
+    lay = layout_3d_ref(*ext) if ref_layout else None
+    p = cs.Plan("box3d1r", ext, w, precision=cs.Precision.SPLIT, layout=lay)
+    p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    x = O.splitmix_uniform(int(np.prod(ext)), 98).reshape(ext)
+    buf = p.pack(x)
+    launches0 = cs.kernel_launch_count()
+    got = split_run(p, buf, 3)
+    assert cs.kernel_launch_count() > launches0
+    ref = oracle_run(p, buf, w, 1, 3)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
 def test_split_tc3d_wide_range():
     """Signed weights and inputs spanning 40 binades inside each tile: the
     split digits are relative to the largest weight and to each input plane's
