@@ -15,13 +15,16 @@ using namespace ff;
 
 unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// Rows per thread of the 7-point star kernel (tile 32 x 8 kStarRows).
+constexpr int kStarRows = 2;
+
 // Planes per CTA of the z-marching 3D kernels: 32 on large grids; fewer on
 // small ones, so that the grid still gives every SM several CTAs (a CTA
 // marches its planes one after another, so a small grid with 32-plane
 // columns would leave most SMs idle and make each sweep a long serial chain).
-int z_chunk(const GridView &g)
+int z_chunk(const GridView &g, int tile_rows = 16)
 {
-    const long long cols = (long long)ceil_div(g.ext[2], 32) * ceil_div(g.ext[1], 16);
+    const long long cols = (long long)ceil_div(g.ext[2], 32) * ceil_div(g.ext[1], tile_rows);
     const long long want = 4LL * device_sm_count();
     long long zc = (g.ext[0] * cols + want - 1) / want;
     return (int)std::max(1LL, std::min(32LL, zc));
@@ -148,84 +151,95 @@ __global__ void __launch_bounds__(256) k3d_ff1(const float2 *__restrict__ in, fl
     }
 }
 
-// The 7-point star (radius 1). A CTA owns a 32 x 16 column of outputs and
-// marches zc planes; thread (lx, ly) computes rows ly and ly + 8 of column lx.
-// The z neighbours of its two outputs stay in registers (planes z-1, z, z+1),
-// plane z+2 is loaded one iteration ahead, and only plane z with its x/y halo
-// goes through shared memory, double buffered so that one barrier per plane
-// suffices: in iteration z the CTA reads buffer z and fills buffer z+1 (its
-// interior from the registers holding plane z+1, its 96-point halo ring from
-// loads issued one iteration earlier by warps 0-2). Taps in the order of
-// k3d_ff1 (z-1, y-1, x-1, centre, x+1, y+1, z+1), so the sums are the same.
+// The 7-point star (radius 1). A CTA owns a 32 x (8 RPT) column of outputs
+// and marches zc planes; thread (lx, ly) computes rows ly, ly + 8, ... of
+// column lx. The z neighbours of its outputs stay in registers (planes z-1,
+// z, z+1), plane z+2 is loaded one iteration ahead, and only plane z with its
+// x/y halo goes through shared memory, double buffered so that one barrier
+// per plane suffices: in iteration z the CTA reads buffer z and fills buffer
+// z+1 (its interior from the registers holding plane z+1, its halo ring from
+// loads issued one iteration earlier by the first 2 + RPT/2 warps). Taps in
+// the order of k3d_ff1 (z-1, y-1, x-1, centre, x+1, y+1, z+1), so the sums
+// are the same.
+template <int RPT>
 __global__ void __launch_bounds__(256) k3d_star1(const float2 *__restrict__ in, float2 *__restrict__ out,
                                                 int h, int m, int n, long long ldy, long long ldz, int zc,
                                                 FW<27> w)
 {
-    constexpr int TX = 32, TY = 16, SX = TX + 2, SY = TY + 2;
+    constexpr int TX = 32, TY = 8 * RPT, SX = TX + 2, SY = TY + 2;
+    constexpr int kHaloWarps = 2 + RPT / 2;  // rows above and below, then the side columns
     __shared__ float2 pl[2][SY][SX];
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
     const int zend = min(z0 + zc, h);
     // Loads stay inside the buffer: coordinates -1 .. m (rows), -1 .. n
     // (columns), -1 .. h (planes) relative to the interior origin.
-    const int x = x0 + lx, ya = y0 + ly, yb = ya + 8;
-    const bool aok = x <= n && ya <= m, bok = x <= n && yb <= m;
-    const float2 *pa = in + (long long)ya * ldy + x, *pb = in + (long long)yb * ldy + x;
-    // Halo ring (edges only; a star reads no corner): warp 0 the row above,
-    // warp 1 the row below, warp 2 the left (lanes 0-15) and right columns.
+    const int x = x0 + lx;
+    const float2 *p0 = in + (long long)(y0 + ly) * ldy + x;
+    bool rok[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) rok[q] = x <= n && y0 + ly + 8 * q <= m;
+    // Halo ring (edges only; a star reads no corner).
     int hy = 0, hx = 0;
-    if (ly == 0) hy = 0, hx = 1 + lx;
-    else if (ly == 1) hy = SY - 1, hx = 1 + lx;
-    else if (ly == 2) hy = 1 + (lx & 15), hx = lx < 16 ? 0 : SX - 1;
-    const bool hown = ly < 3;
+    if (ly == 0) {
+        hy = 0, hx = 1 + lx;
+    } else if (ly == 1) {
+        hy = SY - 1, hx = 1 + lx;
+    } else if (ly < kHaloWarps) {
+        const int k = (ly - 2) * 32 + lx;  // 0 .. 2 TY - 1
+        hy = 1 + (k < TY ? k : k - TY), hx = k < TY ? 0 : SX - 1;
+    }
+    const bool hown = ly < kHaloWarps;
     const int hgy = y0 - 1 + hy, hgx = x0 - 1 + hx;
     const bool hok = hown && hgy <= m && hgx <= n;
     const float2 *ph = in + (long long)hgy * ldy + hgx;
     const float2 zero = make_float2(0.f, 0.f);
     auto ld = [&](bool ok, const float2 *p, int gz) { return (ok && gz <= h) ? p[(long long)gz * ldz] : zero; };
+    auto row = [&](int q) { return p0 + (long long)(8 * q) * ldy; };
 
-    float2 am = ld(aok, pa, z0 - 1), bm = ld(bok, pb, z0 - 1);
-    float2 ac = ld(aok, pa, z0), bc = ld(bok, pb, z0);
-    float2 ap = ld(aok, pa, z0 + 1), bp = ld(bok, pb, z0 + 1);
-    pl[0][ly + 1][lx + 1] = ac;
-    pl[0][ly + 9][lx + 1] = bc;
+    float2 zm[RPT], zk[RPT], zp[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+        zm[q] = ld(rok[q], row(q), z0 - 1);
+        zk[q] = ld(rok[q], row(q), z0);
+        zp[q] = ld(rok[q], row(q), z0 + 1);
+        pl[0][ly + 1 + 8 * q][lx + 1] = zk[q];
+    }
     if (hown) pl[0][hy][hx] = ld(hok, ph, z0);
     float2 hv = ld(hok, ph, z0 + 1);
     __syncthreads();
     int buf = 0;
     for (int z = z0; z < zend; ++z) {
-        const float2 an = ld(aok, pa, z + 2), bn = ld(bok, pb, z + 2);
-        float sh, sl;
+        float2 zn[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) zn[q] = ld(rok[q], row(q), z + 2);
         const float2(*s)[SX] = pl[buf];
-        ff_first(sh, sl, w.hi[4], w.lo[4], am.x, am.y);
-        ff_tap(sh, sl, w.hi[10], w.lo[10], s[ly][lx + 1].x, s[ly][lx + 1].y);
-        ff_tap(sh, sl, w.hi[12], w.lo[12], s[ly + 1][lx].x, s[ly + 1][lx].y);
-        ff_tap(sh, sl, w.hi[13], w.lo[13], ac.x, ac.y);
-        ff_tap(sh, sl, w.hi[14], w.lo[14], s[ly + 1][lx + 2].x, s[ly + 1][lx + 2].y);
-        ff_tap(sh, sl, w.hi[16], w.lo[16], s[ly + 2][lx + 1].x, s[ly + 2][lx + 1].y);
-        ff_tap(sh, sl, w.hi[22], w.lo[22], ap.x, ap.y);
-        const float2 ra = ff_finish(sh, sl);
-        ff_first(sh, sl, w.hi[4], w.lo[4], bm.x, bm.y);
-        ff_tap(sh, sl, w.hi[10], w.lo[10], s[ly + 8][lx + 1].x, s[ly + 8][lx + 1].y);
-        ff_tap(sh, sl, w.hi[12], w.lo[12], s[ly + 9][lx].x, s[ly + 9][lx].y);
-        ff_tap(sh, sl, w.hi[13], w.lo[13], bc.x, bc.y);
-        ff_tap(sh, sl, w.hi[14], w.lo[14], s[ly + 9][lx + 2].x, s[ly + 9][lx + 2].y);
-        ff_tap(sh, sl, w.hi[16], w.lo[16], s[ly + 10][lx + 1].x, s[ly + 10][lx + 1].y);
-        ff_tap(sh, sl, w.hi[22], w.lo[22], bp.x, bp.y);
-        const float2 rb = ff_finish(sh, sl);
-        if (x < n) {
-            if (ya < m) out[(long long)z * ldz + (long long)ya * ldy + x] = ra;
-            if (yb < m) out[(long long)z * ldz + (long long)yb * ldy + x] = rb;
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            const int r = ly + 8 * q;
+            float sh, sl;
+            ff_first(sh, sl, w.hi[4], w.lo[4], zm[q].x, zm[q].y);
+            ff_tap(sh, sl, w.hi[10], w.lo[10], s[r][lx + 1].x, s[r][lx + 1].y);
+            ff_tap(sh, sl, w.hi[12], w.lo[12], s[r + 1][lx].x, s[r + 1][lx].y);
+            ff_tap(sh, sl, w.hi[13], w.lo[13], zk[q].x, zk[q].y);
+            ff_tap(sh, sl, w.hi[14], w.lo[14], s[r + 1][lx + 2].x, s[r + 1][lx + 2].y);
+            ff_tap(sh, sl, w.hi[16], w.lo[16], s[r + 2][lx + 1].x, s[r + 2][lx + 1].y);
+            ff_tap(sh, sl, w.hi[22], w.lo[22], zp[q].x, zp[q].y);
+            const int y = y0 + r;
+            if (x < n && y < m) out[(long long)z * ldz + (long long)y * ldy + x] = ff_finish(sh, sl);
         }
         buf ^= 1;
-        pl[buf][ly + 1][lx + 1] = ap;
-        pl[buf][ly + 9][lx + 1] = bp;
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) pl[buf][ly + 1 + 8 * q][lx + 1] = zp[q];
         if (hown) pl[buf][hy][hx] = hv;
         hv = ld(hok, ph, z + 2);
         __syncthreads();
-        am = ac, bm = bc;
-        ac = ap, bc = bp;
-        ap = an, bp = bn;
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            zm[q] = zk[q];
+            zk[q] = zp[q];
+            zp[q] = zn[q];
+        }
     }
 }
 
@@ -236,8 +250,11 @@ cudaError_t go3d(const GridView &g, const Weights &w, const float2 *in, float2 *
     const int zc = z_chunk(g);
     dim3 grid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 16), ceil_div(g.ext[0], zc));
     if constexpr (R == 1 && P == PAT_STAR) {
-        k3d_star1<<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2], g.pitch[1],
-                                         g.pitch[0], zc, pack_ff<27>(w));
+        constexpr int RPT = kStarRows;
+        const int zs = z_chunk(g, 8 * RPT);
+        dim3 sgrid(ceil_div(g.ext[2], 32), ceil_div(g.ext[1], 8 * RPT), ceil_div(g.ext[0], zs));
+        k3d_star1<RPT><<<sgrid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], (int)g.ext[2], g.pitch[1],
+                                              g.pitch[0], zs, pack_ff<27>(w));
     } else if constexpr (P == PAT_DENSE) {
         constexpr int smem = K * 2 * (8 + 2 * R) * (32 + 2 * R) * (int)sizeof(split::f2x);
         static std::once_flag once;
