@@ -67,6 +67,27 @@ def test_mix_equals_alone_and_oracle():
         assert rel_err(got, _oracle(shape, x, w, steps))[0] <= tol, (shape, x.shape, steps, prec)
 
 
+def test_large_3d_split_request_alone_and_mixed():
+    """A box3d1r split request above ~2M points runs on the 3D tcgen05 kernel:
+    identical alone and beside other requests, and within the split bar of
+    the oracle."""
+    ext = (132, 130, 128)
+    w = O.seeded_weights(27, 300)
+    x = O.splitmix_uniform(int(np.prod(ext)), 301).reshape(ext)
+    others = _mixed_requests(4, seed=9)
+    with cs.Server(streams=4, max_active=8, chunk_steps=8) as srv:
+        ids = [srv.submit(shape, xo, wo, steps, precision=prec) for shape, xo, wo, steps, prec in others]
+        big = srv.submit("box3d1r", x, w, 12, precision=cs.Precision.SPLIT)
+        mixed = srv.wait(big, timeout=120)[0]
+        for i in ids:
+            srv.wait(i, timeout=120)
+    with cs.Server(streams=1, max_active=1, chunk_steps=8) as alone_srv:
+        alone = alone_srv.wait(alone_srv.submit("box3d1r", x, w, 12, precision=cs.Precision.SPLIT),
+                               timeout=120)[0]
+    np.testing.assert_array_equal(mixed, alone)
+    assert rel_err(mixed, _oracle("box3d1r", x, w, 12))[0] <= 1e-10
+
+
 def test_admission_by_hbm_budget_and_oversized_request():
     import torch
     free, _ = torch.cuda.mem_get_info()
