@@ -777,15 +777,18 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
     const size_t bytes = p->layout.bytes;
     const size_t elem_bytes = sizeof(double);
     DevBuf d[2], stage;
+    // Buffers the copy (or the conversion of a whole copied grid) fills
+    // completely need no clearing; the second buffer's halo must be zero.
+    const bool whole = in_elems * elem_bytes == bytes;
     CS_CUDA(cudaMalloc(&d[0].p, bytes));
     CS_CUDA(cudaMalloc(&d[1].p, bytes));
-    CS_CUDA(cudaMemset(d[0].p, 0, bytes));
+    if (!whole) CS_CUDA(cudaMemset(d[0].p, 0, bytes));
     CS_CUDA(cudaMemset(d[1].p, 0, bytes));
     if (p->prec == CS_PREC_FP64) {
         CS_CUDA(cudaMemcpy(d[0].p, host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
     } else {
         CS_CUDA(cudaMalloc(&stage.p, bytes));
-        CS_CUDA(cudaMemset(stage.p, 0, bytes));
+        if (!whole) CS_CUDA(cudaMemset(stage.p, 0, bytes));
         CS_CUDA(cudaMemcpy(stage.p, host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
         s = cs_split_from_fp64(p, (const double *)stage.p, d[0].p, nullptr);
         if (s != CS_OK) return s;
