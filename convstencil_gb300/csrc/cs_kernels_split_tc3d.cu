@@ -28,17 +28,17 @@
 //     N = 32 (5 - d) feeds levels d..4 of the plane's TMEM block: 3 row
 //     offsets x 5 digits = 15 MMAs per input plane and 1024 outputs.
 //   * Each input plane has its own 160-column TMEM block (ring of three,
-//     columns 0, 160, 320), so every plane keeps its own scale. Output plane
-//     z reads block z-1 (dz = 0 columns), block z (dz = 1) and block z+1
-//     (dz = 2); block z-1 has then served its last output and is handed back
-//     to the MMA thread as soon as it is read.
+//     columns 0, 160, 320), so every plane keeps its own scale. The epilogue
+//     reads a block once, as soon as its MMAs are done, hands it back, and
+//     adds its three tap-plane parts to the running sums of output planes
+//     P+1 (dz = 0), P (dz = 1) and P-1 (dz = 2, its last: stored).
 //   * Roles: one warp issues the window loads (four stage buffers), one
 //     thread issues the MMAs, two groups of four warps cut alternate input
 //     planes into digit planes (ring of seven; a plane is too small for
 //     eight warps to share without waiting on each other),
 //     eight warps (a TMEM lane quarter and half of the 8 columns each)
 //     recombine each plane's levels, add the three double-float partial sums
-//     relative to the largest plane scale, scale once and store.
+//     of an output relative to the largest plane scale, scale once and store.
 //
 // Every mbarrier wait is bounded (2 s of %globaltimer). An expired wait is
 // counted in g_tc3d_wait_timeouts; the CTA then waits, again bounded, for the
@@ -337,6 +337,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ------------------------------------------------ epilogue
         // Warp w reads TMEM lanes 32 (w % 4) ..; lane -> D row m = (output
         // row er, block eb); warp half hh takes columns 8 eb + 4 hh .. + 3.
+        // Each input plane's block is read once, as soon as its MMAs are
+        // done, and handed back at once: its three tap-plane partial sums go
+        // to the running sums of the output planes it feeds. Output j of the
+        // column receives input plane j (dz = 0), j+1 (dz = 1) and j+2
+        // (dz = 2) in that order and is stored after the last.
         const int quarter = warp & 3, hh = (warp - kWarpEpi0) >> 2;
         const int mrow = 32 * quarter + lane;
         const int er = mrow >> 3, eb = mrow & 7;
@@ -346,38 +351,43 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int item = first; item < items && ok; item += step) {
             const Item w = item_of(item, tiles_x, tiles_y, zc, h);
             const int xb = w.x0 + 8 * eb + 4 * hh, yy = w.y0 + er;
-            for (int j = 0; j < w.zn; ++j) {
-                // Blocks of input planes q0+j, q0+j+1 (z taps 0 and 1) were
-                // waited for by the previous output, except at the start of
-                // the column; block q0+j+2 is waited for only after block
-                // q0+j has been read and handed back, so the MMAs of the next
-                // plane never wait for this output's last block.
-                for (int q = q0; j == 0 && q <= q0 + 1 && ok; ++q)
-                    ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1);
-                if (!ok) break;
+            // Running sums of outputs p - 2 (a) and p - 1 (b), relative to
+            // 2^ea, 2^eb: the largest input-plane scale seen so far for each
+            // (exact powers of two, so only a final product can round into
+            // subnormals).
+            float ah[4], al[4], bh[4], bl[4];
+            int ea = 0, eb2 = 0;
+            // Adds a tap plane's part (relative to 2^ex) to a running sum.
+            auto add = [](float (&sh)[4], float (&sl)[4], int &se, const float (&h)[4], const float (&l)[4],
+                          int ex) {
+                float ra = 1.0f, rb = 1.0f;
+                if (ex > se) {
+                    ra = ldexpf(1.0f, se - ex);
+                    se = ex;
+                } else {
+                    rb = ldexpf(1.0f, ex - se);
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float s2, e2;
+                    two_sum(sh[c] * ra, h[c] * rb, s2, e2);
+                    sl[c] = sl[c] * ra + (e2 + l[c] * rb);
+                    sh[c] = s2;
+                }
+            };
+            for (int p = 0; p < w.zn + 2; ++p) {
+                const int q = q0 + p;
+                if (!(ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1))) break;
                 tc_fence_after();
-                float ph[3][4], pl[3][4];  // each tap plane's recombined (hi, lo)
-                int exd[3];
+                const int ex = S.scale_exp[q % kScaleRing];
+                float ph[3][4], pl[3][4];  // recombined (hi, lo) per z tap
 #pragma unroll
                 for (int dz = 0; dz < 3; ++dz) {
-                    const int qq = q0 + j + dz;
-                    if (dz == 2) {
-                        if (!(ok = wait(bar(S.blk_full, qq % NBLK), (qq / NBLK) & 1))) break;
-                        tc_fence_after();
-                    }
-                    exd[dz] = S.scale_exp[qq % kScaleRing];
-                    const unsigned col = (unsigned)(NCOL * (qq % NBLK) + 8 * dz + 4 * hh);
+                    const unsigned col = (unsigned)(NCOL * (q % NBLK) + 8 * dz + 4 * hh);
                     float acc[kDigits][4];
 #pragma unroll
                     for (int L = 0; L < kDigits; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
                     tmem_wait_ld();
-                    // Block qq served its last output: it is the z-1 plane
-                    // here, or one of the last planes of the column.
-                    if (dz == 0 || j == w.zn - 1) {
-                        tc_fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(bar(S.blk_empty, qq % NBLK));
-                    }
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
                         float lv[kDigits];
@@ -386,49 +396,41 @@ __global__ void __launch_bounds__(kThreads, 1)
                         recombine(lv, ph[dz][c], pl[dz][c]);
                     }
                 }
-                if (!ok) break;
-                // Partial sums are added relative to the largest input-plane
-                // scale (exact powers of two), and scaled to absolute values
-                // once at the end, so near the bottom of FP32's range only the
-                // final product rounds into subnormals.
-                const int exm = max(exd[0], max(exd[1], exd[2]));
-                float sh[4], sl[4];
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(S.blk_empty, q % NBLK));
+                // z tap 2 of output p - 2 (its last: store), 1 of output p - 1,
+                // 0 of output p (its first).
+                if (p >= 2) {
+                    add(ah, al, ea, ph[2], pl[2], ex);
+                    if (yy < m) {
+                        const float scale = ldexpf(1.0f, ea + sw.ew - 2 * kDigitBits);
+                        float2 res[4];
 #pragma unroll
-                for (int dz = 0; dz < 3; ++dz) {
-                    const float rel = ldexpf(1.0f, exd[dz] - exm);
+                        for (int c = 0; c < 4; ++c) {
+                            float hi, lo;
+                            two_sum(ah[c], al[c], hi, lo);
+                            res[c] = make_float2(hi * scale, lo * scale);
+                        }
+                        float2 *op = out + (long long)(w.zs + p - 2) * ldz + (long long)yy * ldy + xb;
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const float hi = ph[dz][c] * rel, lo = pl[dz][c] * rel;
-                        if (dz == 0) {
-                            sh[c] = hi;
-                            sl[c] = lo;
-                        } else {
-                            float s2, e2;
-                            two_sum(sh[c], hi, s2, e2);
-                            sh[c] = s2;
-                            sl[c] += e2 + lo;
+                        for (int c = 0; c < 4; c += 2) {
+                            if (xb + c + 1 < n)
+                                *reinterpret_cast<float4 *>(op + c) =
+                                    make_float4(res[c].x, res[c].y, res[c + 1].x, res[c + 1].y);
+                            else if (xb + c < n)
+                                op[c] = res[c];
                         }
                     }
                 }
-                if (yy < m) {
-                    const float scale = ldexpf(1.0f, exm + sw.ew - 2 * kDigitBits);
-                    float2 res[4];
+                if (p >= 1 && p - 1 < w.zn) add(bh, bl, eb2, ph[1], pl[1], ex);
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        float hi, lo;
-                        two_sum(sh[c], sl[c], hi, lo);
-                        res[c] = make_float2(hi * scale, lo * scale);
-                    }
-                    float2 *op = out + (long long)(w.zs + j) * ldz + (long long)yy * ldy + xb;
-#pragma unroll
-                    for (int c = 0; c < 4; c += 2) {
-                        if (xb + c + 1 < n)
-                            *reinterpret_cast<float4 *>(op + c) =
-                                make_float4(res[c].x, res[c].y, res[c + 1].x, res[c + 1].y);
-                        else if (xb + c < n)
-                            op[c] = res[c];
-                    }
+                for (int c = 0; c < 4; ++c) {  // rotate: p - 1 becomes p - 2, p starts
+                    ah[c] = bh[c], al[c] = bl[c];
+                    bh[c] = ph[0][c], bl[c] = pl[0][c];
                 }
+                ea = eb2;
+                eb2 = ex;
             }
             q0 += w.zn + 2;
         }
