@@ -674,7 +674,8 @@ def main():
                "h2d_bytes_per_step": round(gbytes / K, 1), "d2h_bytes_per_step": round(gbytes / K, 1),
                "note": f"one {gbytes / 1e6:.0f} MB host->device and device->host copy per {K}-step run "
                        "(the reference wrapper's contract), pinned host buffers, allocation included; "
-                       "median of 3 complete calls"}
+                       "median of 3 complete calls",
+               "calls_ms": [round(t * 1e3, 2) for t in times]}
 
     # ---------------- CPU oracle baseline (bounded sample)
     cpu = None
