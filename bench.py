@@ -125,9 +125,9 @@ class ClockSampler:
 
 
 def seeded_inputs():
-    from oracle import cs_oracle as O  # the shared SplitMix64 restatement
-    x = O.splitmix_uniform(M * N, GRID_SEED).reshape(M, N)
-    w = O.seeded_weights(TAPS, WEIGHT_SEED)
+    from convstencil_gb300 import workload as WL
+    x = WL.splitmix_uniform(M * N, GRID_SEED).reshape(M, N)
+    w = WL.seeded_weights(TAPS, WEIGHT_SEED)
     return x, w
 
 
@@ -244,7 +244,8 @@ def run_all_configs(args):
     1d2r). Reported numbers only; parity is the tests' job."""
     import torch
     import convstencil_gb300 as cs
-    from oracle import cs_oracle as O
+    from convstencil_gb300 import workload as WL
+    from oracle import cs_oracle as O  # the reference kernels' weight layouts (reference legs only)
     from oracle import ref_gpu
     cs.build()
     have_ref = ref_gpu.available()
@@ -274,8 +275,8 @@ def run_all_configs(args):
     for shape, ext, steps in cases:
         info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
         pts = float(np.prod(ext))
-        x = O.splitmix_uniform(int(pts), GRID_SEED).reshape(ext)
-        w = O.seeded_weights(info[1], WEIGHT_SEED)
+        x = WL.splitmix_uniform(int(pts), GRID_SEED).reshape(ext)
+        w = WL.seeded_weights(info[1], WEIGHT_SEED)
         line = {"config": shape, "extent": list(ext), "time_steps": steps}
         p64 = cs.Plan(shape, ext, w)
         host = p64.pack(x)
@@ -377,13 +378,13 @@ def run_kernel_case(args):
     algorithm, `sweeps` sweeps on an m x n grid."""
     import torch
     import convstencil_gb300 as cs
-    from oracle import cs_oracle as O
+    from convstencil_gb300 import workload as WL
     m, n = args.m, args.n
     shape, ext, taps = SHAPE, (m, n), TAPS
     if args.kernel_case == "split_tc3d":
         shape, ext, taps = "box3d1r", (args.h, m, n), 27
-    x = O.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
-    w = O.seeded_weights(taps, WEIGHT_SEED)
+    x = WL.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
+    w = WL.seeded_weights(taps, WEIGHT_SEED)
     algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA,
             "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
             "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC,
@@ -419,7 +420,7 @@ def served_stream(n_requests, rate_hz, seed, dev_index):
     sum 1 and grids uniform [0,1). Returns the server's latency statistics."""
     import threading
     import convstencil_gb300 as cs
-    from oracle import cs_oracle as O
+    from convstencil_gb300 import workload as WL
     rng = np.random.default_rng(seed)
     shapes = ["star2d1r", "box2d3r", "star3d1r", "box3d1r"]
     reqs = []
@@ -432,7 +433,7 @@ def served_stream(n_requests, rate_hz, seed, dev_index):
             ext = tuple(int(v) for v in np.exp(rng.uniform(np.log(32), np.log(256), 3)))
         steps = int(rng.integers(10, 501))
         prec = cs.Precision.SPLIT if rng.random() < 0.5 else cs.Precision.FP64
-        w = O.seeded_weights(info[1], 1000 + i)
+        w = WL.seeded_weights(info[1], 1000 + i)
         x = np.random.default_rng(seed * 7919 + i).random(ext)
         reqs.append((shape, x, w, steps, prec))
     gaps = rng.exponential(1.0 / rate_hz, n_requests)

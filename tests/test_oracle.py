@@ -91,3 +91,12 @@ def test_splitmix_numpy_matches_c():
     O.lib().cso_fill_uniform(a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1000, 42)
     np.testing.assert_array_equal(a, O.splitmix_uniform(1000, 42))
     assert a.min() >= 0.0 and a.max() < 1.0
+
+
+def test_workload_generators_equal_the_oracle_restatement():
+    """The benchmarks' seeded inputs (convstencil_gb300.workload) are bitwise
+    the oracle's SplitMix64 restatement, which the golden fixtures use."""
+    from convstencil_gb300 import workload as WL
+    for n, seed in ((1, 0), (1000, 1), (4097, 2 ** 40 + 7)):
+        np.testing.assert_array_equal(WL.splitmix_uniform(n, seed), O.splitmix_uniform(n, seed))
+    np.testing.assert_array_equal(WL.seeded_weights(49, 2), O.seeded_weights(49, 2))
