@@ -225,14 +225,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             int q = 0;  // input-plane sequence number
             bool ok = true;
             for (int item = first; item < items && ok; item += step) {
-                const Item w = item_of(item, tiles_x, tiles_y, zc, h);
-                for (int p = 0; p < w.zn + 2; ++p, ++q) {
+                const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
+                for (int p = 0; p < wi.zn + 2; ++p, ++q) {
                     const int sb = q % kStages;
                     if (!(ok = wait(bar(S.stage_empty, sb), ((q / kStages) & 1) ^ 1))) break;
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(bar(S.stage_full, sb), kStageBytes);
-                    tma_load_3d(smem_addr(S.stage[sb]), &tmap, map_x + w.x0 - 4, map_y + w.y0 - 1,
-                                map_z + w.zs - 1 + p, bar(S.stage_full, sb));
+                    tma_load_3d(smem_addr(S.stage[sb]), &tmap, map_x + wi.x0 - 4, map_y + wi.y0 - 1,
+                                map_z + wi.zs - 1 + p, bar(S.stage_full, sb));
                     issued = q + 1;
                 }
             }
@@ -246,8 +246,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             int q = 0;
             bool ok = true;
             for (int item = first; item < items && ok; item += step) {
-                const Item w = item_of(item, tiles_x, tiles_y, zc, h);
-                for (int p = 0; p < w.zn + 2; ++p, ++q) {
+                const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
+                for (int p = 0; p < wi.zn + 2; ++p, ++q) {
                     const int slot = q % NPL, blk = q % NBLK;
                     if (!(ok = wait(bar(S.planes_full, slot), (q / NPL) & 1) &&
                                wait(bar(S.blk_empty, blk), ((q / NBLK) & 1) ^ 1)))
@@ -271,8 +271,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         int q = 0;
         bool go = true;
         for (int item = first; item < items && go; item += step) {
-            const Item w = item_of(item, tiles_x, tiles_y, zc, h);
-            for (int p = 0; p < w.zn + 2; ++p, ++q) {
+            const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
+            for (int p = 0; p < wi.zn + 2; ++p, ++q) {
                 if ((q & 1) != grp) continue;
                 const int sb = q % kStages, slot = q % NPL;
                 // (a) window landed? One thread waits, the barrier shares the answer.
@@ -349,8 +349,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         int q0 = 0;  // first input plane of the item
         bool ok = true;
         for (int item = first; item < items && ok; item += step) {
-            const Item w = item_of(item, tiles_x, tiles_y, zc, h);
-            const int xb = w.x0 + 8 * eb + 4 * hh, yy = w.y0 + er;
+            const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
+            const int xb = wi.x0 + 8 * eb + 4 * hh, yy = wi.y0 + er;
             // Running sums of outputs p - 2 (a) and p - 1 (b), relative to
             // 2^ea, 2^eb: the largest input-plane scale seen so far for each
             // (exact powers of two, so only a final product can round into
@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     sh[c] = s2;
                 }
             };
-            for (int p = 0; p < w.zn + 2; ++p) {
+            for (int p = 0; p < wi.zn + 2; ++p) {
                 const int q = q0 + p;
                 if (!(ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1))) break;
                 tc_fence_after();
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                             two_sum(ah[c], al[c], hi, lo);
                             res[c] = make_float2(hi * scale, lo * scale);
                         }
-                        float2 *op = out + (long long)(w.zs + p - 2) * ldz + (long long)yy * ldy + xb;
+                        float2 *op = out + (long long)(wi.zs + p - 2) * ldz + (long long)yy * ldy + xb;
 #pragma unroll
                         for (int c = 0; c < 4; c += 2) {
                             if (xb + c + 1 < n)
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         }
                     }
                 }
-                if (p >= 1 && p - 1 < w.zn) add(bh, bl, eb2, ph[1], pl[1], ex);
+                if (p >= 1 && p - 1 < wi.zn) add(bh, bl, eb2, ph[1], pl[1], ex);
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {  // rotate: p - 1 becomes p - 2, p starts
                     ah[c] = bh[c], al[c] = bl[c];
@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ea = eb2;
                 eb2 = ex;
             }
-            q0 += w.zn + 2;
+            q0 += wi.zn + 2;
         }
     }
 
