@@ -129,13 +129,20 @@ __global__ void __launch_bounds__(256) k2d_ff(const float2 *__restrict__ in, flo
 // same double-float arithmetic as k2d_ff / k1d_ff, so the results are
 // bitwise identical. HBM traffic per step drops by T, compute grows by the
 // recomputed halo (~10-15 % for T = 4).
-template <int R, int P, int T>
+//
+// 2D (radius 1): a tile of (64 - 2T) x 32 outputs, so that every step's
+// region (at most 64 columns) is one 64-wide row of threads, and four row
+// segments of 64 threads. Each thread rolls a 3 x 3 register window down its
+// rows: three shared-memory loads and no index division per output (the
+// small-grid case is issue-bound: 1024^2 star2d1r 202 -> 228 GStencil/s
+// against a thread-per-output mapping of 64 x 32 tiles).
+template <int P, int T>
 __global__ void __launch_bounds__(256) k2d_ff_tb(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                                 int m, int n, long long ld,
-                                                 FW<(2 * R + 1) * (2 * R + 1)> w)
+                                                 int m, int n, long long ld, FW<9> w)
 {
-    constexpr int K = 2 * R + 1, TX = 64, TY = 32, H = R * T;
+    constexpr int H = T, TX = 64 - 2 * T, TY = 32;
     constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
+    static_assert(SX == 64, "one 64-wide row of threads per step region");
     __shared__ float2 buf[2][SY * SX];
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     for (int idx = threadIdx.x; idx < SY * SX; idx += blockDim.x) {
@@ -145,27 +152,42 @@ __global__ void __launch_bounds__(256) k2d_ff_tb(const float2 *__restrict__ in, 
         buf[0][idx] = inside ? in[(long long)gy * ld + gx] : make_float2(0.f, 0.f);
     }
     __syncthreads();
+    const int cx = threadIdx.x & 63, seg = threadIdx.x >> 6;
+    const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
     for (int t = 1; t <= T; ++t) {
         const float2 *src = buf[(t - 1) & 1];
         float2 *dst = buf[t & 1];
-        const int lo = t * R, ry = SY - 2 * lo, rx = SX - 2 * lo;
-        for (int idx = threadIdx.x; idx < ry * rx; idx += blockDim.x) {
-            const int sy = lo + idx / rx, sx = lo + idx % rx;
-            const int gy = y0 - H + sy, gx = x0 - H + sx;
-            float sh = 0.f, sl = 0.f;
-#pragma unroll
-            for (int i = 0; i < K; ++i)
-#pragma unroll
-                for (int j = 0; j < K; ++j)
-                    if (tap2s<P, R>(i, j)) {
-                        const float2 v = src[(sy - R + i) * SX + (sx - R + j)];
-                        ff_tap(sh, sl, w.hi[i * K + j], w.lo[i * K + j], v.x, v.y);
-                    }
-            const bool inside = gy >= 0 && gy < m && gx >= 0 && gx < n;
-            const float2 r = inside ? ff_finish(sh, sl) : make_float2(0.f, 0.f);
-            if (t < T) dst[sy * SX + sx] = r;
-            else if (inside) out[(long long)gy * ld + gx] = r;
+        constexpr int kSegs = 4;
+        const int ry = SY - 2 * t, rx = SX - 2 * t, per = (ry + kSegs - 1) / kSegs;
+        const int r0 = t + seg * per, r1 = min(t + ry, r0 + per);
+        if (cx < rx && r0 < r1) {
+            const int sx = t + cx, gx = x0 - H + sx;
+            const bool xin = gx >= 0 && gx < n;
+            const float2 *col = src + sx;
+            float2 a0 = col[(r0 - 1) * SX - 1], a1 = col[(r0 - 1) * SX], a2 = col[(r0 - 1) * SX + 1];
+            float2 b0 = col[r0 * SX - 1], b1 = col[r0 * SX], b2 = col[r0 * SX + 1];
+            for (int sy = r0; sy < r1; ++sy) {
+                const float2 *row = col + (sy + 1) * SX;
+                const float2 c0 = row[-1], c1 = row[0], c2 = row[1];
+                float sh = 0.f, sl = 0.f;
+                if (tap2s<P, 1>(0, 0)) ff_tap(sh, sl, w.hi[0], w.lo[0], a0.x, a0.y);
+                if (tap2s<P, 1>(0, 1)) ff_tap(sh, sl, w.hi[1], w.lo[1], a1.x, a1.y);
+                if (tap2s<P, 1>(0, 2)) ff_tap(sh, sl, w.hi[2], w.lo[2], a2.x, a2.y);
+                if (tap2s<P, 1>(1, 0)) ff_tap(sh, sl, w.hi[3], w.lo[3], b0.x, b0.y);
+                if (tap2s<P, 1>(1, 1)) ff_tap(sh, sl, w.hi[4], w.lo[4], b1.x, b1.y);
+                if (tap2s<P, 1>(1, 2)) ff_tap(sh, sl, w.hi[5], w.lo[5], b2.x, b2.y);
+                if (tap2s<P, 1>(2, 0)) ff_tap(sh, sl, w.hi[6], w.lo[6], c0.x, c0.y);
+                if (tap2s<P, 1>(2, 1)) ff_tap(sh, sl, w.hi[7], w.lo[7], c1.x, c1.y);
+                if (tap2s<P, 1>(2, 2)) ff_tap(sh, sl, w.hi[8], w.lo[8], c2.x, c2.y);
+                const int gy = y0 - H + sy;
+                const bool inside = xin && gy >= 0 && gy < m;
+                const float2 r = inside ? ff_finish(sh, sl) : zero;
+                if (t < T) dst[sy * SX + sx] = r;
+                else if (inside) out[(long long)gy * ld + gx] = r;
+                a0 = b0, a1 = b1, a2 = b2;
+                b0 = c0, b1 = c1, b2 = c2;
+            }
         }
         if (t < T) __syncthreads();
     }
@@ -460,11 +482,11 @@ cudaError_t launch_split_sweep_tb(const GridView &g, int R, int P, int T, const 
         CS_TB1(1, 2) CS_TB1(1, 3) CS_TB1(1, 4) CS_TB1(2, 2) CS_TB1(2, 3) CS_TB1(2, 4)
 #undef CS_TB1
     } else if (g.dims == 2 && R == 1) {
-        dim3 grid(ceil_div(g.ext[1], 64), ceil_div(g.ext[0], 32));
 #define CS_TB2(PP, TT)                                                                        \
     if (P == PP && T == TT) {                                                                 \
-        k2d_ff_tb<1, PP, TT><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1],      \
-                                                   g.pitch[0], pack_ff<9>(w));                \
+        dim3 grid(ceil_div(g.ext[1], 64 - 2 * TT), ceil_div(g.ext[0], 32));                   \
+        k2d_ff_tb<PP, TT><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1],         \
+                                                 g.pitch[0], pack_ff<9>(w));                  \
         return cudaGetLastError();                                                            \
     }
         CS_TB2(PAT_STAR, 2) CS_TB2(PAT_STAR, 3) CS_TB2(PAT_STAR, 4)
