@@ -11,6 +11,7 @@
 // captured once as a CUDA graph and replayed on later calls.
 #include "../../include/convstencil.h"
 #include "cs_internal.h"
+#include "cs_split_ff.cuh"
 
 #include <algorithm>
 #include <map>
@@ -48,13 +49,7 @@ struct Item {
 
 constexpr int TX = 64, TY = 32, RPT = 8;
 
-__host__ __device__ constexpr int iabs_b(int x) { return x < 0 ? -x : x; }
-
-template <int P, int R>
-__host__ __device__ constexpr bool tapb(int i, int j)
-{
-    return P == PAT_DENSE ? true : P == PAT_STAR ? (i == R || j == R) : (iabs_b(i - R) + iabs_b(j - R) <= R);
-}
+using cs::ff::tap2s;
 
 __device__ __forceinline__ int find_item(const Item *items, int nitems, int tile)
 {
@@ -108,7 +103,7 @@ __global__ void __launch_bounds__(256) k2d_fma_batch(const Item *__restrict__ it
                 if (o >= 0 && o < RPT) {
 #pragma unroll
                     for (int j = 0; j < K; ++j)
-                        if (tapb<P, R>(i, j)) acc[o] = fma(ws[i * K + j], v[j], acc[o]);
+                        if (tap2s<P, R>(i, j)) acc[o] = fma(ws[i * K + j], v[j], acc[o]);
                 }
             }
         }
@@ -122,26 +117,6 @@ __global__ void __launch_bounds__(256) k2d_fma_batch(const Item *__restrict__ it
 }
 
 // Split precision, double-float on FP32 cores: the k2d_ff<R,P> body.
-__device__ __forceinline__ void two_sum_b(float a, float b, float &s, float &e)
-{
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-__device__ __forceinline__ void ff_tap_b(float &sh, float &sl, float wh, float wl, float xh, float xl)
-{
-    const float p = wh * xh;
-    const float ep = fmaf(wh, xh, -p);
-    float s, q;
-    two_sum_b(sh, p, s, q);
-    sh = s;
-    sl += q;
-    sl += ep;
-    sl = fmaf(wh, xl, sl);
-    sl = fmaf(wl, xh, sl);
-}
-
 template <int R, int P>
 __global__ void __launch_bounds__(256) k2d_ff_batch(const Item *__restrict__ items, int nitems,
                                                     const float2 *__restrict__ wtab, int total)
@@ -182,9 +157,10 @@ __global__ void __launch_bounds__(256) k2d_ff_batch(const Item *__restrict__ ite
                 if (o >= 0 && o < RPT) {
 #pragma unroll
                     for (int j = 0; j < K; ++j)
-                        if (tapb<P, R>(i, j)) {
+                        if (tap2s<P, R>(i, j)) {
                             const float2 wv = ws[i * K + j];
-                            ff_tap_b(sh[o], sl[o], wv.x, wv.y, v[j].x, v[j].y);
+                            cs::ff::ff_acc(i * K + j == cs::ff::first_tap2<P, R>(), sh[o], sl[o], wv.x, wv.y,
+                                           v[j].x, v[j].y);
                         }
                 }
             }
@@ -195,7 +171,7 @@ __global__ void __launch_bounds__(256) k2d_ff_batch(const Item *__restrict__ ite
             const int y = y0 + g * RPT + o, x = x0 + c;
             if (y < I.m && x < I.n) {
                 float h, l;
-                two_sum_b(sh[o], sl[o], h, l);
+                cs::split::two_sum(sh[o], sl[o], h, l);
                 out[(long long)y * I.ld + x] = make_float2(h, l);
             }
         }

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k1d_ff(const float2 *__restrict__ in, flo
         const int lx = threadIdx.x + p * 256;
         float sh = 0.f, sl = 0.f;
 #pragma unroll
-        for (int t = 0; t <= 2 * R; ++t) ff_tap(sh, sl, w.hi[t], w.lo[t], s[lx + t].x, s[lx + t].y);
+        for (int t = 0; t <= 2 * R; ++t) ff_acc(t == 0, sh, sl, w.hi[t], w.lo[t], s[lx + t].x, s[lx + t].y);
         const long long gx = x0 + lx;
         if (gx < n) out[gx] = ff_finish(sh, sl);
     }
@@ -109,7 +109,8 @@ __global__ void __launch_bounds__(256) k2d_ff(const float2 *__restrict__ in, flo
 #pragma unroll
                 for (int j = 0; j < K; ++j)
                     if (tap2s<P, R>(i, j))
-                        ff_tap(sh[o], sl[o], w.hi[i * K + j], w.lo[i * K + j], v[j].x, v[j].y);
+                        ff_acc(i * K + j == first_tap2<P, R>(), sh[o], sl[o], w.hi[i * K + j],
+                               w.lo[i * K + j], v[j].x, v[j].y);
             }
         }
     }
@@ -154,6 +155,7 @@ __global__ void __launch_bounds__(256) k2d_ff_tb(const float2 *__restrict__ in, 
     __syncthreads();
     const int cx = threadIdx.x & 63, seg = threadIdx.x >> 6;
     const float2 zero = make_float2(0.f, 0.f);
+    constexpr int kFirst = first_tap2<P, 1>();
 #pragma unroll
     for (int t = 1; t <= T; ++t) {
         const float2 *src = buf[(t - 1) & 1];
@@ -171,15 +173,15 @@ __global__ void __launch_bounds__(256) k2d_ff_tb(const float2 *__restrict__ in, 
                 const float2 *row = col + (sy + 1) * SX;
                 const float2 c0 = row[-1], c1 = row[0], c2 = row[1];
                 float sh = 0.f, sl = 0.f;
-                if (tap2s<P, 1>(0, 0)) ff_tap(sh, sl, w.hi[0], w.lo[0], a0.x, a0.y);
-                if (tap2s<P, 1>(0, 1)) ff_tap(sh, sl, w.hi[1], w.lo[1], a1.x, a1.y);
-                if (tap2s<P, 1>(0, 2)) ff_tap(sh, sl, w.hi[2], w.lo[2], a2.x, a2.y);
-                if (tap2s<P, 1>(1, 0)) ff_tap(sh, sl, w.hi[3], w.lo[3], b0.x, b0.y);
-                if (tap2s<P, 1>(1, 1)) ff_tap(sh, sl, w.hi[4], w.lo[4], b1.x, b1.y);
-                if (tap2s<P, 1>(1, 2)) ff_tap(sh, sl, w.hi[5], w.lo[5], b2.x, b2.y);
-                if (tap2s<P, 1>(2, 0)) ff_tap(sh, sl, w.hi[6], w.lo[6], c0.x, c0.y);
-                if (tap2s<P, 1>(2, 1)) ff_tap(sh, sl, w.hi[7], w.lo[7], c1.x, c1.y);
-                if (tap2s<P, 1>(2, 2)) ff_tap(sh, sl, w.hi[8], w.lo[8], c2.x, c2.y);
+                if (tap2s<P, 1>(0, 0)) ff_acc(0 == kFirst, sh, sl, w.hi[0], w.lo[0], a0.x, a0.y);
+                if (tap2s<P, 1>(0, 1)) ff_acc(1 == kFirst, sh, sl, w.hi[1], w.lo[1], a1.x, a1.y);
+                if (tap2s<P, 1>(0, 2)) ff_acc(2 == kFirst, sh, sl, w.hi[2], w.lo[2], a2.x, a2.y);
+                if (tap2s<P, 1>(1, 0)) ff_acc(3 == kFirst, sh, sl, w.hi[3], w.lo[3], b0.x, b0.y);
+                if (tap2s<P, 1>(1, 1)) ff_acc(4 == kFirst, sh, sl, w.hi[4], w.lo[4], b1.x, b1.y);
+                if (tap2s<P, 1>(1, 2)) ff_acc(5 == kFirst, sh, sl, w.hi[5], w.lo[5], b2.x, b2.y);
+                if (tap2s<P, 1>(2, 0)) ff_acc(6 == kFirst, sh, sl, w.hi[6], w.lo[6], c0.x, c0.y);
+                if (tap2s<P, 1>(2, 1)) ff_acc(7 == kFirst, sh, sl, w.hi[7], w.lo[7], c1.x, c1.y);
+                if (tap2s<P, 1>(2, 2)) ff_acc(8 == kFirst, sh, sl, w.hi[8], w.lo[8], c2.x, c2.y);
                 const int gy = y0 - H + sy;
                 const bool inside = xin && gy >= 0 && gy < m;
                 const float2 r = inside ? ff_finish(sh, sl) : zero;
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(256) k1d_ff_tb(const float2 *__restrict__ in, 
 #pragma unroll
             for (int j = 0; j < 2 * R + 1; ++j) {
                 const float2 v = src[sx - R + j];
-                ff_tap(sh, sl, w.hi[j], w.lo[j], v.x, v.y);
+                ff_acc(j == 0, sh, sl, w.hi[j], w.lo[j], v.x, v.y);
             }
             const bool inside = gx >= 0 && gx < n;
             const float2 r = inside ? ff_finish(sh, sl) : make_float2(0.f, 0.f);

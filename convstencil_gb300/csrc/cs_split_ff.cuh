@@ -97,6 +97,26 @@ __host__ __device__ constexpr bool tap2s(int i, int j)
     return P == PAT_DENSE ? true : P == PAT_STAR ? (i == R || j == R) : (iabs_(i - R) + iabs_(j - R) <= R);
 }
 
+// Row-major index of the first tap of a 2D pattern: the tap that starts
+// each output's sum (ff_first instead of ff_tap).
+template <int P, int R>
+__host__ __device__ constexpr int first_tap2()
+{
+    for (int i = 0; i < 2 * R + 1; ++i)
+        for (int j = 0; j < 2 * R + 1; ++j)
+            if (tap2s<P, R>(i, j)) return i * (2 * R + 1) + j;
+    return 0;
+}
+
+// ff_first for the first tap of a sum, ff_tap for the others.
+__device__ __forceinline__ void ff_acc(bool first, float &sh, float &sl, float wh, float wl, float xh, float xl)
+{
+    if (first)
+        ff_first(sh, sl, wh, wl, xh, xl);
+    else
+        ff_tap(sh, sl, wh, wl, xh, xl);
+}
+
 template <int P, int R>
 __host__ __device__ constexpr bool tap3s(int a, int i, int j)
 {
