@@ -424,7 +424,8 @@ cs_status choose_time_block(cs_plan *p, int algo, const void *a, void *b, cudaSt
         for (int t = 1; t <= 4; ++t) {
             CS_CUDA(cudaEventRecord(e0, st));
             cudaError_t e = t == 1 ? cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, 0, in, o, st)
-                                   : cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w, in, o, st);
+                                   : cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w, in, o,
+                                                               st);
             if (e != cudaSuccess) return cuda_fail(e, "time-block tuning launch");
             CS_CUDA(cudaEventRecord(e1, st));
             CS_CUDA(cudaEventSynchronize(e1));
@@ -579,7 +580,8 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
     case CS_OPT_TIME_BLOCK:
         if (v < 0 || v > 4) return fail(CS_ERR_INVALID_ARGUMENT, "time block must be 0 (tuner) or 1..4");
         if (v > 1 && !(p->prec == CS_PREC_SPLIT && cs::split_tb_supported(p->dims, p->radius, p->pattern)))
-            return fail(CS_ERR_UNSUPPORTED, "temporal blocking serves split-precision 2D radius-1 and 1D plans");
+            return fail(CS_ERR_UNSUPPORTED,
+                        "temporal blocking serves split-precision 2D radius-1 and 1D plans");
         p->time_block = (int)v;
         return CS_OK;
     }
@@ -683,7 +685,8 @@ CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *str
         CS_CUDA(cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal));
         const long long before = cs::g_launches.load();
         cudaError_t e = cudaSuccess;
-        for (int k = 0; k < glaunches && e == cudaSuccess; ++k) e = one_launch(tb, c ^ (k & 1), p->capture_stream);
+        for (int k = 0; k < glaunches && e == cudaSuccess; ++k)
+            e = one_launch(tb, c ^ (k & 1), p->capture_stream);
         cs::note_launch(before - cs::g_launches.load());  // captured, not run: counted at each replay
         cudaGraph_t g = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &g);
