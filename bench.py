@@ -47,7 +47,7 @@ TAPS = 49
 GRID_SEED, WEIGHT_SEED = 1, 2
 METRIC = "GStencil/s (split-prec vs FP64, same GB300, stated err); served p50/p99 latency"
 WORKLOAD = "box2d3r 8192x8192 float64, 49 seeded weights normalised to sum 1, zero halo radius 3"
-FP64_PEAK_TFLOPS = 1.05  # measured DMMA/DFMA ceiling on GB300, profiles/fp64_pipe_peak_gb300.md
+FP64_PEAK_TFLOPS = 1.05  # DMMA/DFMA ceiling measured on GB300 by `bench.py --pipe-peaks`
 
 
 def env_rank():
