@@ -82,6 +82,16 @@ def test_plan_validation_without_gpu():
                                                         "elements": 100})
     with pytest.raises(cs.ConvStencilError):   # MMA algo only for FP64 2D radius-3 dense
         cs.Plan("star2d1r", (8, 8), np.ones(5)).set_option(cs.Option.ALGO, cs.Algo.FP64_MMA)
+    # tcgen05: split plans of 2D radius 3 and of 3D radius 1 (27 weights)
+    cs.Plan("box3d1r", (8, 8, 8), np.full(27, 1 / 27),
+            precision=cs.Precision.SPLIT).set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    cs.Plan("box2d3r", (8, 8), np.full(49, 1 / 49),
+            precision=cs.Precision.SPLIT).set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    with pytest.raises(cs.ConvStencilError):   # fused 3D plans are radius 3
+        cs.Plan("box3d1r", (8, 8, 8), np.full(196, 1 / 196), semantics=cs.Semantics.FUSED,
+                precision=cs.Precision.SPLIT).set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    with pytest.raises(cs.ConvStencilError):   # split algorithms need a split plan
+        cs.Plan("box3d1r", (8, 8, 8), np.full(27, 1 / 27)).set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
 
 
 def test_pack_unpack_roundtrip():
