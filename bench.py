@@ -6,23 +6,30 @@ the whole grid). Default: 1000 steps, the workload's full length.
 
   value    GStencil/s of the split-precision path (FP32 hi+lo grids, exact FP16
            slices on the tcgen05 tensor cores), device-resident, K steps timed with CUDA
-           events on the launching stream. The FP64 path (same GPU) is timed
-           the same way and reported under "fp64"; the split result's error
-           against the FP64 path is stated under "err".
-  e2e      the same K steps through the reference-shaped C ABI with HOST
-           buffers (cs_gpu_box_2d3r for FP64, cs_run_host for split): device
+           events on the launching stream. The FP64 path (same GPU, the kernel
+           the plan's tuner picks: the FP64-accurate tcgen05 digit pipeline on
+           this GPU) is timed the same way and reported under "fp64".
+  err      the split result against the FP64 path after K steps; err_vs_oracle
+           both paths against the FP64 CPU oracle over the whole grid after
+           min(K, 100) steps.
+  e2e      the same K steps through the C ABI with HOST buffers (cs_run_host
+           for split; fp64.e2e: the reference-shaped cs_gpu_box_2d3r): device
            allocation, host->device copy, K sweeps, device->host copy inside
            the timed region.
   roofline the dominant kernel's achieved rate over its measured peak.
   cpu_baseline  the CPU oracle (OpenMP C restatement of the reference's
            naive stencil) on the host cores, on a bounded sample.
+  served   a Poisson request stream through the server (latency), and the same
+           mix submitted at once, split-only vs FP64-only (served throughput).
 
---impl reference runs the reference's CPU stencil path (the oracle port, all
-host cores) on the same workload and prints its own line. --configs measures
-every BASELINE configuration (FP64, split, and the reference's own kernels on
-this GPU) and prints one line per configuration.
+--impl reference runs the reference's own CPU stencil (naive_box2d1r, built
+from its sources on this host by oracle/build_ref.sh; the oracle port if it
+was not built) on all host threads and prints its own line. --configs
+measures every BASELINE configuration (FP64, split, and the reference's own
+kernels on this GPU) and prints one line per configuration.
 Under torchrun with N ranks each rank runs an independent replica (the
 reference has no multi-GPU path; replicas only), value = N * work / max time.
+A run in which a bounded device-side wait expired prints no value.
 """
 from __future__ import annotations
 
@@ -47,7 +54,7 @@ TAPS = 49
 GRID_SEED, WEIGHT_SEED = 1, 2
 METRIC = "GStencil/s (split-prec vs FP64, same GB300, stated err); served p50/p99 latency"
 WORKLOAD = "box2d3r 8192x8192 float64, 49 seeded weights normalised to sum 1, zero halo radius 3"
-FP64_PEAK_TFLOPS = 1.05  # DMMA/DFMA ceiling measured on GB300 by `bench.py --pipe-peaks`
+PEAKS_EXE = os.path.join(ROOT, "convstencil_gb300", "_lib", "pipe_peaks")
 
 
 def env_rank():
@@ -61,6 +68,23 @@ def load_peaks():
             return json.load(f), "measured"
     except OSError:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def pipe_peaks():
+    """Arithmetic-pipe rates measured now on this GPU (bench_pipe_peaks.cu,
+    built by build()): {"fp64 fma": TFLOP/s, ...}; {} if unavailable."""
+    try:
+        out = subprocess.run([PEAKS_EXE, "--json"], capture_output=True, text=True, timeout=120).stdout
+        return json.loads(out.strip().splitlines()[-1])
+    except (OSError, ValueError, IndexError, subprocess.SubprocessError):
+        return {}
+
+
+def bench_config(K, world):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD, "m": M, "n": N, "time_steps": K,
+            "l2": "inputs larger than L2 (537 MB per grid vs 129 MB L2)",
+            "parallelism": f"replicas x{world}"}
 
 
 def profile_traffic(kernel_key):
@@ -146,24 +170,88 @@ def oracle_sample(x, w, rows, steps, threads=None):
 
 
 # ----------------------------------------------------------------- reference
+def reference_naive_2d():
+    """The reference's own naive_box2d1r (src/2d/main.cu:57-115) with C linkage,
+    built from its sources on this host by oracle/build_ref.sh (harness
+    oracle/ref_harness/ref_naive_2d.cu); None when it was not built."""
+    path = os.path.join(ROOT, "oracle", "_ref", "libref_naive_2d.so")
+    if not os.path.exists(path):
+        return None
+    try:
+        L = ctypes.CDLL(path)
+    except OSError:
+        return None
+    P = ctypes.POINTER(ctypes.c_double)
+    L.ref_naive_box2d1r.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
+    L.ref_naive_box2d1r.restype = None
+    return L
+
+
+def reference_sweep(L, a, b, w, rows, threads):
+    """One sweep of the reference's naive stencil a -> b over the first `rows`
+    interior rows of (M+6) x (N+8) grids, on `threads` host threads: each calls
+    the reference function on its own slab of rows (slabs share only read-only
+    halo rows; ctypes releases the GIL during the call)."""
+    ld = N + 8
+    P = ctypes.POINTER(ctypes.c_double)
+    wp = w.ctypes.data_as(P)
+    per = (rows + threads - 1) // threads
+
+    def work(t):
+        r0, r1 = t * per, min(rows, (t + 1) * per)
+        if r1 > r0:
+            off = r0 * ld * 8
+            L.ref_naive_box2d1r(ctypes.cast(a.ctypes.data + off, P), ctypes.cast(b.ctypes.data + off, P), wp,
+                                r1 - r0 + 6, ld)
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    from oracle import cs_oracle as O
-    O.build()
     x, w = seeded_inputs()
+    w = np.ascontiguousarray(w)
     cores = os.cpu_count() or 1
-    # Calibrate a slab so one step is ~max(0.05, budget/(K+W)) seconds.
-    t, _ = oracle_sample(x, w, 256, 1)
-    per_row = t / 256
+    L = reference_naive_2d()
     budget = 90.0
-    rows = int(max(64, min(M, budget / max(1, args.steps + args.warmup) / per_row)))
-    for _ in range(args.warmup):
-        oracle_sample(x, w, rows, 1)
+    if L is not None:
+        kind = "reference"
+        what = "the reference's naive_box2d1r (src/2d/main.cu:57-115), built from its sources on this host"
+        ld = N + 8
+        a = np.zeros((M + 6, ld))
+        a[3:M + 3, 4:N + 4] = x
+        b = np.zeros_like(a)
+        t0 = time.perf_counter()
+        reference_sweep(L, a, b, w, 512, cores)
+        per_row = (time.perf_counter() - t0) / 512
+        rows = int(max(64, min(M, budget / max(1, args.steps + args.warmup) / per_row)))
+
+        def step(i):
+            src, dst = (a, b) if i % 2 == 0 else (b, a)
+            t = time.perf_counter()
+            reference_sweep(L, src, dst, w, rows, cores)
+            return time.perf_counter() - t, rows * N
+    else:
+        from oracle import cs_oracle as O
+        O.build()
+        kind = "port"
+        what = "the oracle's OpenMP restatement of the reference's naive stencil (reference build unavailable)"
+        t, _ = oracle_sample(x, w, 256, 1)
+        rows = int(max(64, min(M, budget / max(1, args.steps + args.warmup) / (t / 256))))
+
+        def step(i):
+            return oracle_sample(x, w, rows, 1)
+    for i in range(args.warmup):
+        step(i)
     tot_t, tot_pts = 0.0, 0
-    for _ in range(args.steps):
-        t, pts = oracle_sample(x, w, rows, 1)
+    for i in range(args.steps):
+        t, pts = step(args.warmup + i)
         tot_t += t
         tot_pts += pts
     val = tot_pts / tot_t / 1e9
@@ -171,11 +259,11 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "GStencil/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (SplitMix64 seeded)",
-        "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": args.steps,
-                   "sample": f"each step = one sweep over a {rows} x {N} slab"},
-        "cpu_baseline": {"value": round(val, 4), "unit": "GStencil/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} sweeps of a {rows}x{N} slab, OpenMP on {cores} threads"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (SplitMix64 seeded grid and weights)",
+        "config": bench_config(args.steps, world),
+        "cpu_baseline": {"value": round(val, 4), "unit": "GStencil/s", "cores": cores, "kind": kind,
+                         "sample": f"each step = one sweep of {what} over a {rows} x {N} slab of the grid, "
+                                   f"{cores} host threads"},
         "e2e": {"value": round(val, 4), "unit": "GStencil/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -363,13 +451,10 @@ def _reference_config(ref_gpu, O, shape, ext, steps):
 
 # ------------------------------------------------------------ pipe peaks
 def run_pipe_peaks():
-    """FP64 / FP32 / tensor pipe issue rates (convstencil_gb300/csrc/peaks/pipe_peaks.cu)."""
+    """FP64 / FP32 / tensor / integer pipe rates (bench_pipe_peaks.cu, built by build())."""
     from convstencil_gb300 import build_lib
-    src = os.path.join(ROOT, "convstencil_gb300", "csrc", "peaks", "pipe_peaks.cu")
-    exe = os.path.join(ROOT, "convstencil_gb300", "_lib", "pipe_peaks")
-    os.makedirs(os.path.dirname(exe), exist_ok=True)
-    subprocess.check_call([build_lib.nvcc()] + build_lib.ARCH + ["-O3", "-o", exe, src])
-    return subprocess.call([exe])
+    build_lib.build()
+    return subprocess.call([PEAKS_EXE])
 
 
 # ------------------------------------------------------------ ncu cases
@@ -385,7 +470,7 @@ def run_kernel_case(args):
         shape, ext, taps = "box3d1r", (args.h, m, n), 27
     x = WL.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
     w = WL.seeded_weights(taps, WEIGHT_SEED)
-    algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA,
+    algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA, "fp64_tc": cs.Algo.FP64_TC,
             "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
             "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC,
             "split_tc3d": cs.Algo.SPLIT_TC}[args.kernel_case]
@@ -412,12 +497,13 @@ def run_kernel_case(args):
 
 
 # ------------------------------------------------------------ served stream
-def served_stream(n_requests, rate_hz, seed, dev_index):
+def served_stream(n_requests, rate_hz, seed, dev_index, precision=None):
     """BASELINE config 5 as a bounded sample: n_requests with Poisson arrivals
-    (rate_hz), shape uniform over {star2d1r, box2d3r, star3d1r, box3d1r}, 2D
-    sides log-uniform 64..4096, 3D sides log-uniform 32..256, steps uniform
-    10..500, half FP64 and half split precision, seeded weights normalised to
-    sum 1 and grids uniform [0,1). Returns the server's latency statistics."""
+    (rate_hz; None = all submitted at once, the saturated form), shape uniform
+    over {star2d1r, box2d3r, star3d1r, box3d1r}, 2D sides log-uniform
+    64..4096, 3D sides log-uniform 32..256, steps uniform 10..500, half FP64
+    and half split precision (or all `precision`), seeded weights normalised
+    to sum 1 and grids uniform [0,1). Returns the server's statistics."""
     import threading
     import convstencil_gb300 as cs
     from convstencil_gb300 import workload as WL
@@ -433,10 +519,12 @@ def served_stream(n_requests, rate_hz, seed, dev_index):
             ext = tuple(int(v) for v in np.exp(rng.uniform(np.log(32), np.log(256), 3)))
         steps = int(rng.integers(10, 501))
         prec = cs.Precision.SPLIT if rng.random() < 0.5 else cs.Precision.FP64
+        if precision is not None:
+            prec = precision
         w = WL.seeded_weights(info[1], 1000 + i)
         x = np.random.default_rng(seed * 7919 + i).random(ext)
         reqs.append((shape, x, w, steps, prec))
-    gaps = rng.exponential(1.0 / rate_hz, n_requests)
+    gaps = rng.exponential(1.0 / rate_hz, n_requests) if rate_hz else np.zeros(n_requests)
     srv = cs.Server(streams=8, max_active=32, hbm_fraction=0.5, chunk_steps=32)
     ids = [None] * n_requests
     lat = [None] * n_requests
@@ -460,11 +548,12 @@ def served_stream(n_requests, rate_hz, seed, dev_index):
     th.join()
     st = srv.stats()
     srv.close()
-    return {"requests": n_requests, "arrival_rate_hz": rate_hz,
+    mix = {None: "50% split", cs.Precision.SPLIT: "all split", cs.Precision.FP64: "all FP64"}[precision]
+    return {"requests": n_requests, "arrival_rate_hz": rate_hz if rate_hz else "all at once",
             "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
             "mean_ms": round(st["mean_s"] * 1e3, 3), "gstencil_s": round(st["gstencil_s"], 3),
-            "completed": st["completed"], "failed": st["failed"],
-            "mix": "star2d1r/box2d3r/star3d1r/box3d1r, 2D 64-4096, 3D 32-256, steps 10-500, 50% split"}
+            "wall_s": round(st["wall_s"], 3), "completed": st["completed"], "failed": st["failed"],
+            "mix": "star2d1r/box2d3r/star3d1r/box3d1r, 2D 64-4096, 3D 32-256, steps 10-500, " + mix}
 
 
 # ---------------------------------------------------------------------- ours
@@ -478,12 +567,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the whole-grid oracle comparison")
     ap.add_argument("--served", type=int, default=96,
                     help="requests in the served-stream sample (0 = skip)")
     ap.add_argument("--served-rate", type=float, default=40.0, help="Poisson arrival rate (req/s)")
+    ap.add_argument("--saturated", type=int, default=48,
+                    help="requests per precision in the saturated served comparison (0 = skip)")
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the served stream (--served requests at --served-rate) and the "
+                         "saturated comparison, print their line and exit")
     ap.add_argument("--kernel-case", default=None,
-                    choices=["fp64_fma", "fp64_mma", "split_mma", "split_mma_tma", "split_fma", "split_tc",
-                             "split_tc3d"],
+                    choices=["fp64_fma", "fp64_mma", "fp64_tc", "split_mma", "split_mma_tma", "split_fma",
+                             "split_tc", "split_tc3d"],
                     help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid (split_tc3d: "
                          "box3d1r on --h x --m x --n) (small cases for ncu captures) and exit")
     ap.add_argument("--m", type=int, default=4608)
@@ -561,7 +656,19 @@ def main():
         return ev0.elapsed_time(ev1) / 1e3 / reps
 
     results = {}
-    # ---------------- FP64 path
+    results = {}
+    pts = float(M) * N
+    peaks_now = pipe_peaks()  # measured now, on this GPU
+
+    if args.served_only:
+        line = {"served": served_stream(args.served, args.served_rate, 17 + rank, local) if args.served else None}
+        if args.saturated:
+            line["served_saturated"] = saturated_served(args.saturated, local)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
+
+    # ---------------- FP64 path (the drop-in form; the plan's tuner picks the kernel)
     p64 = cs.Plan(SHAPE, (M, N), w)
     host = p64.pack(x)
     a64 = torch.from_numpy(host).to(dev)
@@ -575,9 +682,8 @@ def main():
             t64, in_b64, l64 = timed_device_run(p64, a64, b64, K)
         t64 = max_over_ranks(t64)
         res64 = (b64 if in_b64 else a64).clone()  # kept: the sweeps below reuse a64/b64
-        results["fp64"] = {"seconds": t64, "launches": l64, "clocks": cl64.summary()}
-        k64 = kernel_avg_seconds(p64, a64, b64)
-        results["fp64"]["kernel_s"] = k64
+        results["fp64"] = {"seconds": t64, "launches": l64, "clocks": cl64.summary(), "algo": p64.algo.name}
+        results["fp64"]["kernel_s"] = kernel_avg_seconds(p64, a64, b64)
 
     # ---------------- split path
     split_ok = True
@@ -601,82 +707,115 @@ def main():
         out_sp = torch.zeros(psp.elements, dtype=torch.float64, device=dev)
         psp.split_to_fp64(sb if in_bsp else sa, out_sp, stream=stream)
         torch.cuda.synchronize()
-        results["split"] = {"seconds": tsp, "launches": lsp, "clocks": clsp.summary()}
+        results["split"] = {"seconds": tsp, "launches": lsp, "clocks": clsp.summary(), "algo": psp.algo.name}
         results["split"]["kernel_s"] = kernel_avg_seconds(psp, sa, sb)
         if "fp64" in results:
-            ref = res64
-            d = (out_sp - ref).abs()
-            scale = ref.abs().max()
-            den = torch.clamp(ref.abs(), min=float(scale) * 1e-3)
-            results["split"]["err_vs_fp64"] = {
-                "max_rel": float((d / den).max()), "mean_rel": float((d / den).mean()),
-                "normwise": float(d.max() / scale)}
-        del raw, s0
+            results["split"]["err_vs_fp64"] = err_stats(out_sp, res64)
 
     headline = "split" if "split" in results else "fp64"
     hr = results[headline]
-    pts = float(M) * N
     value = world * pts * K / hr["seconds"] / 1e9
+    pk_hbm = float(peaks["hbm_gbs"])
 
-    # ---------------- roofline of the dominant kernel
-    if headline == "fp64":
-        flops = 2.0 * TAPS * pts
-        ach = flops / hr["kernel_s"] / 1e12
-        roof = {"bound": "tensor", "achieved": round(ach, 4), "peak": FP64_PEAK_TFLOPS,
-                "unit": "TFLOP/s", "frac": round(ach / FP64_PEAK_TFLOPS, 4),
-                "traffic": profile_traffic("fp64_box2d3r_sweep"),
-                "kernel": "k2d_fma<3,dense>", "peak_source": "FP64 pipe microbenchmark (DFMA=DMMA pipe)",
-                "algorithmic": f"{2 * TAPS} FLOP/pt x {M}x{N} pts per launch"}
-    else:
-        byts = 16.0 * pts
-        ach = byts / hr["kernel_s"] / 1e9
-        pk = float(peaks["hbm_gbs"])
-        roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": pk, "unit": "GB/s",
-                "frac": round(ach / pk, 4),
-                "traffic": profile_traffic("split_tc_box2d3r_sweep" if psp.algo == cs.Algo.SPLIT_TC
-                                           else "split_box2d3r_sweep"),
-                "kernel": f"split sweep ({psp.algo.name})",
-                "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+    def hbm_roof(kernel_s, kernel, profile_key):
+        ach = 16.0 * pts / kernel_s / 1e9
+        return {"bound": "hbm", "achieved": round(ach, 1), "peak": pk_hbm, "unit": "GB/s",
+                "frac": round(ach / pk_hbm, 4), "traffic": profile_traffic(profile_key),
+                "traffic_source": f"profiles/{profile_key}.md (ncu dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum per launch)",
+                "kernel": kernel, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs, of measured)",
                 "algorithmic": f"16 B/pt (8 B read + 8 B write) x {M}x{N} pts per launch"}
 
-    # ---------------- e2e through the reference-shaped C ABI (host buffers)
-    e2e = None
+    # ---------------- roofline of the dominant kernel
+    if headline == "split":
+        roof = hbm_roof(hr["kernel_s"], f"split sweep ({psp.algo.name})",
+                        "split_tc_box2d3r_sweep" if psp.algo == cs.Algo.SPLIT_TC else "split_box2d3r_sweep")
+    else:
+        roof = fp64_roof(results["fp64"], pts, peaks_now, hbm_roof)
+
+    # ---------------- error against the FP64 CPU oracle over the whole grid
+    err_oracle = None
+    if rank == 0 and not args.no_oracle:
+        check = min(K, 100)
+        from oracle import cs_oracle as O  # the checker, never the thing measured
+        O.build()
+        L = p64.layout.as_dict()
+        ld = L["pitch"][0]
+        t0 = time.perf_counter()
+        ref = torch.from_numpy(O.run_2d(host.reshape(-1, ld), w, 3, M, N, L["origin"] // ld, L["origin"] % ld,
+                                        check).reshape(-1))
+        oracle_s = time.perf_counter() - t0
+        err_oracle = {"steps": check, "oracle_seconds": round(oracle_s, 2),
+                      "oracle": "OpenMP C restatement of the reference's naive stencil, whole grid"}
+        if check == K:
+            fin64 = res64 if "fp64" in results else None
+            finsp = out_sp if split_ok else None
+        else:  # fresh runs of `check` steps from the seeded grid
+            fin64 = finsp = None
+            if "fp64" in results:
+                a64.copy_(torch.from_numpy(host))
+                b64.zero_()
+                fin64 = (b64 if p64.run(a64, b64, check, stream=stream) else a64).clone()
+            if split_ok:
+                sa.copy_(s0)
+                sb.zero_()
+                fin = sb if psp.run(sa, sb, check, stream=stream) else sa
+                finsp = torch.zeros(psp.elements, dtype=torch.float64, device=dev)
+                psp.split_to_fp64(fin, finsp, stream=stream)
+            torch.cuda.synchronize()
+        if fin64 is not None:
+            err_oracle["fp64"] = err_stats(fin64.cpu(), ref, p64.interior_index())
+        if finsp is not None:
+            err_oracle["split"] = err_stats(finsp.cpu(), ref, p64.interior_index())
+        del ref
+
+    # ---------------- e2e through the C ABI (host buffers)
+    e2e = e2e64 = None
     if not args.no_e2e:
-        pin_in = torch.from_numpy(host).pin_memory()
-        pin_out = torch.empty_like(pin_in).pin_memory()
-        L = cs.lib()
+        L_ = cs.lib()
         dp = ctypes.POINTER(ctypes.c_double)
-        pin_p = ctypes.cast(pin_in.data_ptr(), dp)
-        out_p = ctypes.cast(pin_out.data_ptr(), dp)
         wp = np.ascontiguousarray(w)
-        if headline != "split":
+
+        def median_call(fn):
+            times = []
+            for _ in range(3):
+                barrier()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                times.append(max_over_ranks(time.perf_counter() - t0))
+            barrier()
+            return statistics.median(times), times
+
+        gbytes = float(host.nbytes)
+        if split_ok:
+            pin_in = torch.from_numpy(host).pin_memory()
+            pin_out = torch.empty_like(pin_in).pin_memory()
+            te, times = median_call(lambda: cs.check(L_.cs_run_host(psp._h, ctypes.cast(pin_in.data_ptr(), dp),
+                                                                   ctypes.cast(pin_out.data_ptr(), dp), K)))
+            e2e = {"value": round(world * pts * K / te / 1e9, 4), "unit": "GStencil/s",
+                   "h2d_bytes_per_step": round(gbytes / K, 1), "d2h_bytes_per_step": round(gbytes / K, 1),
+                   "note": f"cs_run_host: one {gbytes / 1e6:.0f} MB FP64 host->device and device->host copy per "
+                           f"{K}-step run, pinned host buffers, allocation and FP64<->(hi, lo) conversion "
+                           "included; median of 3 complete calls",
+                   "calls_ms": [round(t * 1e3, 2) for t in times]}
+            del pin_in, pin_out
+        if "fp64" in results:
             # cs_gpu_box_2d3r takes the reference layout (m+6) x (n+8)
             ref_in = np.zeros((M + 6, N + 8))
             ref_in[3:M + 3, 4:N + 4] = x
             ref_pin = torch.from_numpy(ref_in.reshape(-1)).pin_memory()
             ref_out = torch.empty_like(ref_pin).pin_memory()
-        # Three complete calls (allocation, copies, K steps each); the median.
-        times = []
-        for _ in range(3):
-            barrier()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            if headline == "split":
-                cs.check(L.cs_run_host(psp._h, pin_p, out_p, K))
-            else:
-                cs.check(L.cs_gpu_box_2d3r(ctypes.cast(ref_pin.data_ptr(), dp),
-                                           ctypes.cast(ref_out.data_ptr(), dp),
-                                           wp.ctypes.data_as(dp), K, M, N))
-            times.append(max_over_ranks(time.perf_counter() - t0))
-        te = statistics.median(times)
-        barrier()
-        gbytes = float(host.nbytes)
-        e2e = {"value": round(world * pts * K / te / 1e9, 4), "unit": "GStencil/s",
-               "h2d_bytes_per_step": round(gbytes / K, 1), "d2h_bytes_per_step": round(gbytes / K, 1),
-               "note": f"one {gbytes / 1e6:.0f} MB host->device and device->host copy per {K}-step run "
-                       "(the reference wrapper's contract), pinned host buffers, allocation included; "
-                       "median of 3 complete calls",
-               "calls_ms": [round(t * 1e3, 2) for t in times]}
+            te, times = median_call(lambda: cs.check(L_.cs_gpu_box_2d3r(
+                ctypes.cast(ref_pin.data_ptr(), dp), ctypes.cast(ref_out.data_ptr(), dp), wp.ctypes.data_as(dp),
+                K, M, N)))
+            rb = float(ref_in.nbytes)
+            e2e64 = {"value": round(world * pts * K / te / 1e9, 4), "unit": "GStencil/s",
+                     "h2d_bytes_per_step": round(rb / K, 1), "d2h_bytes_per_step": round(rb / K, 1),
+                     "note": "cs_gpu_box_2d3r (the reference wrapper's signature and layout), host buffers, "
+                             "allocation included; median of 3 complete calls",
+                     "calls_ms": [round(t * 1e3, 2) for t in times]}
+            del ref_pin, ref_out
 
     # ---------------- CPU oracle baseline (bounded sample)
     cpu = None
@@ -690,12 +829,22 @@ def main():
         cpu = {"value": round(work / t / 1e9, 4), "unit": "GStencil/s", "cores": cores, "kind": "port",
                "sample": f"1 sweep of a {rows}x{N} slab of the same grid (OpenMP C oracle)"}
 
-    served = None
+    served = saturated = None
     if args.served > 0:
         served = served_stream(args.served, args.served_rate, 17 + rank, local)
+    if args.saturated > 0:
+        saturated = saturated_served(args.saturated, local)
 
+    # Bounded device-side waits that expired anywhere in this run leave
+    # outputs incomplete: no value is printed then.
+    expired = cs.device_wait_timeouts(reset=False)
     if rank != 0:
         return 0
+    if expired:
+        print(json.dumps({"metric": METRIC, "value": None, "unit": "GStencil/s",
+                          "error": f"{expired} bounded device-side wait(s) expired during the run; "
+                                   "results incomplete, no value reported"}), flush=True)
+        return 3
     clocks = hr["clocks"]
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "GStencil/s", "n_gpus": world,
@@ -703,24 +852,63 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32x2 split (exact fp16 slices, f32 accum)" if headline == "split" else "f64",
         "data": "synthetic (SplitMix64 seeded grid and weights)",
-        "config": {"workload": WORKLOAD, "m": M, "n": N, "time_steps": K, "precision": headline,
-                   "l2": "inputs larger than L2 (537 MB per grid vs 129 MB L2)",
-                   "parallelism": f"replicas x{world}"},
-        "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "served": served,
-        "gpu_launches": hr["launches"], "clocks": clocks,
+        "config": bench_config(K, world),
+        "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "served": served, "served_saturated": saturated,
+        "gpu_launches": hr["launches"], "clocks": clocks, "headline_kernel": hr["algo"],
     }
     if "fp64" in results:
         r = results["fp64"]
         line["fp64"] = {"value": round(world * pts * K / r["seconds"] / 1e9, 4), "unit": "GStencil/s",
-                        "ms_per_step": round(r["seconds"] / K * 1e3, 4),
+                        "algo": r["algo"], "ms_per_step": round(r["seconds"] / K * 1e3, 4),
                         "kernel_ms": round(r["kernel_s"] * 1e3, 4), "launches": r["launches"],
-                        "clocks": r["clocks"]}
+                        "clocks": r["clocks"], "roofline": fp64_roof(r, pts, peaks_now, hbm_roof), "e2e": e2e64}
     if "split" in results and "err_vs_fp64" in results["split"]:
         line["err"] = results["split"]["err_vs_fp64"]
+    line["err_vs_oracle"] = err_oracle
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def err_stats(got, ref, interior=None):
+    """Max / mean pointwise relative error (denominator floored at 1e-3 *
+    max|ref|) and the normwise error, over the interior."""
+    import torch
+    g = got.reshape(-1).double().cpu() if hasattr(got, "reshape") else torch.as_tensor(got)
+    r = ref.reshape(-1).double().cpu()
+    if interior is not None:
+        idx = torch.from_numpy(np.ascontiguousarray(interior.reshape(-1)))
+        g, r = g[idx], r[idx]
+    d = (g - r).abs()
+    scale = float(r.abs().max())
+    den = torch.clamp(r.abs(), min=scale * 1e-3)
+    return {"max_rel": float((d / den).max()), "mean_rel": float((d / den).mean()),
+            "normwise": float(d.max() / scale)}
+
+
+def fp64_roof(r, pts, peaks_now, hbm_roof):
+    """Roofline of the FP64 path's kernel: HBM for the tcgen05 digit pipeline
+    (no FP64 instruction), the FP64 pipe (measured now) for the FMA/MMA ones."""
+    if r["algo"] == "FP64_TC":
+        return hbm_roof(r["kernel_s"], "k2d_tc<FmtF64> (FP64_TC)", "fp64_tc_box2d3r_sweep")
+    pk = peaks_now.get("fp64 fma")
+    ach = 2.0 * TAPS * pts / r["kernel_s"] / 1e12
+    return {"bound": "fp64 pipe", "achieved": round(ach, 4), "peak": pk, "unit": "TFLOP/s",
+            "frac": round(ach / pk, 4) if pk else None, "kernel": r["algo"],
+            "peak_source": "FP64 FMA rate measured in this run (bench_pipe_peaks.cu)",
+            "algorithmic": f"{2 * TAPS} FLOP/pt x {M}x{N} pts per launch"}
+
+
+def saturated_served(n, local):
+    """The config-5 mix with every request submitted at once: served split-only
+    vs FP64-only throughput (GStencil/s of completed requests over the wall
+    time) and their ratio."""
+    import convstencil_gb300 as cs
+    sp = served_stream(n, None, 23, local, precision=cs.Precision.SPLIT)
+    fp = served_stream(n, None, 23, local, precision=cs.Precision.FP64)
+    ratio = round(sp["gstencil_s"] / fp["gstencil_s"], 3) if fp["gstencil_s"] else None
+    return {"split": sp, "fp64": fp, "split_over_fp64": ratio}
 
 
 if __name__ == "__main__":

@@ -78,12 +78,15 @@ class Algo(enum.IntEnum):
     SPLIT_FMA = 4
     SPLIT_MMA_TMA = 5
     SPLIT_TC = 6
+    FP64_TC = 7
 
 
 class Option(enum.IntEnum):
     ALGO = 0
     REANCHOR_INTERVAL = 2
     TIME_BLOCK = 3
+    WAIT_LIMIT_US = 4
+    WAIT_TEST_SKIP_LOADS = 5
 
 
 class Layout(ctypes.Structure):

@@ -3,7 +3,9 @@
 Compiles every CUDA translation unit under csrc/ in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo`` and links one
 shared library in-tree (``convstencil_gb300/_lib/``), plus the drop-in CLIs
-(``convstencil_gb300/_lib/convstencil_{1d,2d,3d}``). No cmake, no torch.
+(``convstencil_gb300/_lib/convstencil_{1d,2d,3d}``) and the bench's
+arithmetic-pipe microbenchmark (``_lib/pipe_peaks`` from bench_pipe_peaks.cu).
+No cmake, no torch.
 """
 from __future__ import annotations
 
@@ -45,7 +47,7 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 
 def _headers() -> list[str]:
-    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     inc = os.path.join(ROOT, "include")
     hs += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return hs
@@ -87,6 +89,12 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError(f"CLI build failed for {name}:\n{r.stdout}\n{r.stderr}")
+    peaks_src = os.path.join(ROOT, "bench_pipe_peaks.cu")
+    peaks_exe = os.path.join(OUT, "pipe_peaks")
+    if os.path.exists(peaks_src) and _stale(peaks_exe, [peaks_src]):
+        r = subprocess.run([nvcc()] + ARCH + ["-O3", "-o", peaks_exe, peaks_src], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"pipe_peaks build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         print("built", LIB)
     return LIB

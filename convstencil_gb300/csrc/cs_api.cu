@@ -226,6 +226,7 @@ struct cs_plan {
     int time_block = 0;            // split FMA: steps per launch (0 = tuner)
     int last_time_block = 1;
     long long reanchor = 100;
+    cs::TcWait wait;               // bounded waits of the tcgen05 kernels
     // Small grids: blocks of sweeps replayed as CUDA graphs (see cs_run).
     std::mutex graph_mu;
     std::map<std::tuple<const void *, const void *, int, int, int>, cudaGraphExec_t> graphs;
@@ -255,6 +256,15 @@ bool split_mma_ok(const cs_plan *p)
            cs::split_mma_layout_ok(p->view, p->layout.origin);
 }
 
+// FP64 plans of 2D radius-3 stencils (any 7x7 weights) also run on the
+// tcgen05 digit pipeline; like the split slice kernels its error is relative
+// to the tile's scale, so grids smaller than the 8x8 window stay on FP64 FMA.
+bool fp64_tc_ok(const cs_plan *p)
+{
+    return p->prec == CS_PREC_FP64 && p->dims == 2 && p->radius == 3 && p->view.ext[0] >= 8 &&
+           p->view.ext[1] >= 8 && cs::split_mma_layout_ok(p->view, p->layout.origin);
+}
+
 // Split plans of 3D radius-1 stencils (27 weights) also run on the tcgen05
 // slice kernel.
 bool split_tc3d_ok(const cs_plan *p)
@@ -270,6 +280,10 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
         const double *in = (const double *)in_base + off;
         double *out = (double *)out_base + off;
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(p->view, p->w, in, out, st);
+        if (algo == CS_ALGO_FP64_TC && fp64_tc_ok(p) && reinterpret_cast<uintptr_t>(out_base) % 16 == 0 &&
+            cs::split_tma_layout_ok(p->view, off, in_base))
+            return cs::launch_fp64_sweep_tc(p->view, p->w, off, p->layout.elements, (const double *)in_base,
+                                            (double *)out_base, p->wait, st);
         return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st);
     }
     // The tensor-core split kernels store float4 (two points) at even element
@@ -281,13 +295,13 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
         if (algo == CS_ALGO_SPLIT_TC && split_tc3d_ok(p) &&
             cs::split_tc3d_layout_ok(p->view, off, in_base, out_base))
             return cs::launch_split_sweep_tc3d(p->view, p->w, off, p->layout.elements,
-                                               (const float2 *)in_base, (float2 *)out_base, st);
+                                               (const float2 *)in_base, (float2 *)out_base, p->wait, st);
         algo = CS_ALGO_SPLIT_FMA;
     }
     const bool tma_ok = out16 && cs::split_tma_layout_ok(p->view, off, in_base);
     if (algo == CS_ALGO_SPLIT_TC && tma_ok)
         return cs::launch_split_sweep_tc(p->view, p->w, off, p->layout.elements,
-                                         (const float2 *)in_base, (float2 *)out_base, st);
+                                         (const float2 *)in_base, (float2 *)out_base, p->wait, st);
     if (algo == CS_ALGO_SPLIT_MMA_TMA && tma_ok)
         return cs::launch_split_sweep_tma(p->view, p->w, off, p->layout.elements,
                                           (const float2 *)in_base, (float2 *)out_base, st);
@@ -339,16 +353,17 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
         cand[nc++] = CS_ALGO_SPLIT_MMA_TMA;
         cand[nc++] = CS_ALGO_SPLIT_FMA;
     } else {
-        if (p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) {
-            *out = CS_ALGO_FP64_MMA;
+        if ((p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) || (p->algo == CS_ALGO_FP64_TC && fp64_tc_ok(p))) {
+            *out = p->algo;
             return CS_OK;
         }
-        if (p->algo != CS_ALGO_AUTO || !fp64_mma_ok(p)) {
+        if (p->algo != CS_ALGO_AUTO || (!fp64_mma_ok(p) && !fp64_tc_ok(p))) {
             *out = CS_ALGO_FP64_FMA;
             return CS_OK;
         }
         cand[nc++] = CS_ALGO_FP64_FMA;
-        cand[nc++] = CS_ALGO_FP64_MMA;
+        if (fp64_mma_ok(p)) cand[nc++] = CS_ALGO_FP64_MMA;
+        if (fp64_tc_ok(p)) cand[nc++] = CS_ALGO_FP64_TC;
     }
     auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
     {
@@ -553,15 +568,18 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
     if (!p) return fail(CS_ERR_INVALID_ARGUMENT, "plan is NULL");
     switch (opt) {
     case CS_OPT_ALGO:
-        if (v < CS_ALGO_AUTO || v > CS_ALGO_SPLIT_TC) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
+        if (v < CS_ALGO_AUTO || v > CS_ALGO_FP64_TC) return fail(CS_ERR_INVALID_ARGUMENT, "bad algo");
         if ((v == CS_ALGO_SPLIT_MMA || v == CS_ALGO_SPLIT_FMA || v == CS_ALGO_SPLIT_MMA_TMA ||
              v == CS_ALGO_SPLIT_TC) &&
             p->prec != CS_PREC_SPLIT)
             return fail(CS_ERR_INVALID_ARGUMENT, "split algo needs a split-precision plan");
-        if ((v == CS_ALGO_FP64_FMA || v == CS_ALGO_FP64_MMA) && p->prec != CS_PREC_FP64)
+        if ((v == CS_ALGO_FP64_FMA || v == CS_ALGO_FP64_MMA || v == CS_ALGO_FP64_TC) && p->prec != CS_PREC_FP64)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
         if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
+        if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p))
+            return fail(CS_ERR_UNSUPPORTED,
+                        "FP64 tcgen05 serves 2D radius-3 FP64 plans of at least 8x8 on even-aligned layouts");
         if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
             p->algo = (int)v;
             return CS_OK;
@@ -583,6 +601,15 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
             return fail(CS_ERR_UNSUPPORTED,
                         "temporal blocking serves split-precision 2D radius-1 and 1D plans");
         p->time_block = (int)v;
+        return CS_OK;
+    case CS_OPT_WAIT_LIMIT_US:
+        if (v < 1 || v > 60000000LL)
+            return fail(CS_ERR_INVALID_ARGUMENT, "wait limit must be 1 .. 60,000,000 microseconds");
+        p->wait.limit_ns = (unsigned long long)v * 1000ull;
+        return CS_OK;
+    case CS_OPT_WAIT_TEST_SKIP_LOADS:
+        if (v != 0 && v != 1) return fail(CS_ERR_INVALID_ARGUMENT, "skip-loads test hook is 0 or 1");
+        p->wait.skip_loads = (int)v;
         return CS_OK;
     }
     return fail(CS_ERR_INVALID_ARGUMENT, "unknown option %d", (int)opt);
@@ -796,6 +823,12 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
         s = cs_split_from_fp64(p, (const double *)stage.p, d[0].p, nullptr);
         if (s != CS_OK) return s;
     }
+    // Bounded device-side waits that expire during this call leave outputs
+    // unwritten; the counters before and after tell (any expiry in the
+    // process during the call counts).
+    unsigned waits_before = 0, waits_after = 0;
+    s = cs_device_wait_timeouts(&waits_before, 0);
+    if (s != CS_OK) return s;
     cudaEvent_t e0, e1;
     CS_CUDA(cudaEventCreate(&e0));
     CS_CUDA(cudaEventCreate(&e1));
@@ -815,6 +848,11 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
     cudaEventDestroy(e1);
     if (loop_seconds) *loop_seconds = ms * 1e-3;
     t_loop_seconds = ms * 1e-3;
+    s = cs_device_wait_timeouts(&waits_after, 0);
+    if (s != CS_OK) return s;
+    if (waits_after != waits_before)
+        return fail(CS_ERR_TIMEOUT, "%u bounded device-side wait(s) expired during the run; the result is incomplete",
+                    waits_after - waits_before);
     const void *res = d[in_b].p;
     if (p->prec == CS_PREC_SPLIT) {
         s = cs_split_to_fp64(p, res, (double *)stage.p, nullptr);

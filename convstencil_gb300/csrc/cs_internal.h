@@ -64,11 +64,22 @@ bool split_tma_layout_ok(const GridView &g, long long origin, const void *base);
 cudaError_t launch_split_sweep_tma(const GridView &g, const Weights &w, long long origin,
                                    long long elements, const float2 *in_base, float2 *out_base,
                                    cudaStream_t stream);
+// Bounded device-side waits of the tcgen05 kernels, per launch.
+struct TcWait {
+    unsigned long long limit_ns = 2000000000ull;  // bound of one mbarrier wait
+    int skip_loads = 0;  // test hook: issue no TMA loads, so the first wait runs out
+};
 // tcgen05 slice kernel with TMEM accumulators (cs_kernels_split_tc.cu); same
 // layout conditions as the TMA variant.
 cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long origin,
                                   long long elements, const float2 *in_base, float2 *out_base,
-                                  cudaStream_t stream);
+                                  const TcWait &wait, cudaStream_t stream);
+// The same pipeline on FP64 grids (2D dense 7x7): six exact 9-bit digits per
+// operand cut from the FP64 bits by integer operations, exact FP32 level sums
+// on tcgen05, integer recombination to FP64. Layout conditions as above.
+cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long origin, long long elements,
+                                 const double *in_base, double *out_base, const TcWait &wait,
+                                 cudaStream_t stream);
 // 2D tensor map over a whole (hi, lo) buffer of `rows` x `ld` pairs, box_x x box_y tiles.
 cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long long ld, long long rows,
                                     unsigned box_x, unsigned box_y);
@@ -83,7 +94,7 @@ cudaError_t encode_split_window_map_3d(CUtensorMap *map, const float2 *base, lon
 bool split_tc3d_layout_ok(const GridView &g, long long origin, const void *in_base, const void *out_base);
 cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
                                     long long elements, const float2 *in_base, float2 *out_base,
-                                    cudaStream_t stream);
+                                    const TcWait &wait, cudaStream_t stream);
 int device_sm_count();
 // Bounded device-side waits that expired since the last reset (TMA/mma.sync
 // kernel, 2D and 3D tcgen05 kernels).

@@ -1,20 +1,34 @@
-// cs_kernels_split_tc.cu — split-precision sweep for dense 7x7 kernels on
-// the fifth-generation tensor cores (tcgen05.mma, accumulators in TMEM).
+// cs_kernels_split_tc.cu — dense 7x7 sweeps on the fifth-generation tensor
+// cores (tcgen05.mma, accumulators in TMEM), in two number formats that share
+// one pipeline:
 //
-// Arithmetic: as in the mma.sync slice kernel (cs_kernels_split.cu). Every
-// input (hi, lo) pair of a tile is scaled by a power of two and cut into five
-// balanced 9-bit digits held exactly in FP16; the weights are cut the same
-// way. Products of digit k of x and digit e of w with k + e = L land in one
-// FP32 accumulator per level L. Every product is an integer below 2^16 and a
-// level sums at most 49 * 5 of them, so each level is exact (< 2^24) whatever
-// the summation order; the five levels are recombined error-free into a new
-// (hi, lo) pair.
+//   * split precision (FmtSplit): grids of FP32 (hi, lo) pairs. Every input
+//     pair of a tile is scaled by a power of two and cut into five balanced
+//     9-bit digits held exactly in FP16; the weights likewise. Products of
+//     digit k of x and digit e of w with k + e = L land in one FP32
+//     accumulator per level L. Every product is an integer below 2^16 and a
+//     level sums at most 49 * 5 of them, so each level is exact (< 2^24)
+//     whatever the summation order; the five levels are recombined
+//     error-free into a new (hi, lo) pair.
+//   * FP64 (FmtF64): FP64 grids, the drop-in form. Each FP64 input is turned
+//     into a 52-bit fixed-point integer relative to its tile's largest
+//     exponent and cut into six balanced 9-bit digits with integer
+//     operations only (no FP64 instruction: this GPU's FP64 pipe runs at
+//     about 1/1000 of its FP16 tensor rate); the weights into six digits of a
+//     fixed point below 1/4, so the top digits of both stay within 128.
+//     Levels 0..5 (21 digit pairs per tap) are kept: level L sums at most
+//     49 * (4 * 2^16 + 2 * 2^15) < 2^24, so each is again exact. The levels
+//     are combined into one 64-bit integer and rounded once to FP64 by
+//     integer operations. Error per sweep: the inputs carry 52 bits below
+//     the tile maximum, the weights 53 below the largest weight, and the
+//     dropped levels >= 6 weigh below 2^-48 of (tile max x largest weight)
+//     in the worst case (about 2^-53 for data without adversarial digits).
 //
 // Mapping onto tcgen05 (M = 128, K = 16, N = 32 per level):
 //   * A CTA owns a 64 x 64 output tile: 16 row groups of 4 rows, 8 blocks
 //     of 8 columns. Its input window (70 x 72 points, columns x0-4 ..
-//     x0+67) arrives by one 2D TMA load and is cut into five digit planes
-//     in shared memory, one row of 72 halves (144 bytes) per window row.
+//     x0+67) arrives by one 2D TMA load and is cut into digit planes in
+//     shared memory, one row of 72 halves (144 bytes) per window row.
 //   * Row m of the A operand is the 16-wide window of block b = m % 8 in
 //     row group r = m / 8. A K-major, non-swizzled shared-memory descriptor
 //     with a 16-byte K-chunk stride and a stride of four plane rows between
@@ -24,29 +38,31 @@
 //     no im2col copy exists.
 //   * Column n of B_i is output (row 4r + rho, column 8b + c), n = 8 rho + c;
 //     B_i[k][n] = w[i - rho][k - c - 1] where that tap exists, else 0.
-//   * For input digit d the B operand is [B_i(e=0) | ... | B_i(e=4-d)] (the
-//     first 32 (5-d) rows of one K-major matrix) and the accumulator starts
-//     at TMEM column 32 d, so one MMA feeds levels d..4 at once: per tile
-//     10 offsets x 5 digits = 50 MMAs into 160 FP32 columns.
+//   * For input digit d the B operand is [B_i(e=0) | ... | B_i(e=D-1-d)]
+//     (the first 32 (D-d) rows of one K-major matrix) and the accumulator
+//     starts at TMEM column 32 d, so one MMA feeds levels d..D-1 at once:
+//     per tile 10 offsets x D digits MMAs (50 split, 60 FP64) into 32 D FP32
+//     columns.
 //   * The tile shape serves as many outputs per MMA as shared memory allows:
-//     4 rows per group give 4096 outputs per 50 MMAs (2 rows: 2048 per 40).
-//     The issuing thread stalls on each MMA until the tensor core accepts
-//     it, so the 50 MMAs are unrolled with compile-time descriptor offsets
-//     (measured on GB300: 56 cycles per MMA for this N = 160..32 sequence,
-//     70 with the descriptors computed in the loop).
-//   * One persistent CTA per SM (about 188 KB of shared memory) with warp
-//     roles joined by mbarriers: one warp issues the TMA window loads, one
-//     thread issues the MMAs (tcgen05.mma issue blocks while the tensor
-//     core is busy, so it must not sit in anyone else's barrier), eight
-//     warps read a window into registers, release the stage to the next
-//     load and cut the digit planes, and eight warps drain the accumulators,
-//     recombine and store. Two accumulators (TMEM columns 0 and 256) and two
-//     sets of digit planes let slicing of tile t+1, the MMAs of tile t and
-//     the stores of tile t-1 run at the same time.
+//     4 rows per group give 4096 outputs per tile (2 rows: 2048 per 40
+//     MMAs). The issuing thread stalls on each MMA until the tensor core
+//     accepts it, so the MMAs are unrolled with compile-time descriptor
+//     offsets (measured on GB300: 56 cycles per MMA for the split N =
+//     160..32 sequence, 70 with the descriptors computed in the loop).
+//   * One persistent CTA per SM (about 188 KB of shared memory split, 218 KB
+//     FP64) with warp roles joined by mbarriers: one warp issues the TMA
+//     window loads, one thread issues the MMAs (tcgen05.mma issue blocks
+//     while the tensor core is busy, so it must not sit in anyone else's
+//     barrier), eight warps read a window into registers, release the stage
+//     to the next load and cut the digit planes, and eight warps drain the
+//     accumulators, recombine and store. Two accumulators (TMEM columns 0 and
+//     256) and two sets of digit planes let slicing of tile t+1, the MMAs of
+//     tile t and the stores of tile t-1 run at the same time.
 //
-// Every mbarrier wait is bounded (2 s of %globaltimer). An expired wait is
-// counted in g_tc_wait_timeouts; the CTA then waits, again bounded, for the
-// TMA copy and the MMAs it still has in flight, frees its TMEM and leaves.
+// Every mbarrier wait is bounded (WaitCfg, 2 s by default). An expired wait
+// is counted in g_tc_wait_timeouts; the CTA then waits, again bounded, for
+// the TMA copy and the MMAs it still has in flight, frees its TMEM and
+// leaves.
 #include "cs_internal.h"
 #include "cs_split_common.cuh"
 #include "cs_tc_common.cuh"
@@ -54,7 +70,9 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
+#include <type_traits>
 
 namespace cs {
 
@@ -63,11 +81,112 @@ __device__ unsigned int g_tc_wait_timeouts;
 namespace {
 
 using split::kDigitBits;
-using split::kDigits;
-using split::SliceWeights;
 using split::slice_digits;
 using split::two_sum;
 using namespace tc;
+
+// Number formats.
+struct FmtSplit {
+    static constexpr bool kF64 = false;
+    static constexpr int kDigits = split::kDigits;  // 5
+    using Out = float2;
+    using Digits = split::SliceWeights;
+};
+
+// Six balanced base-512 digits of w / 2^ew (|w| / 2^ew < 1/4, so the top
+// digit stays within 128) for the 49 taps of a 7x7 kernel.
+struct F64Weights {
+    __half d[6][49];
+    int ew;
+};
+
+struct FmtF64 {
+    static constexpr bool kF64 = true;
+    static constexpr int kDigits = 6;
+    using Out = double;
+    using Digits = F64Weights;
+};
+
+F64Weights f64_slice_weights(const Weights &w)
+{
+    F64Weights s{};
+    double mx = 0.0;
+    for (int i = 0; i < 49; ++i) mx = std::fmax(mx, std::fabs(w.v[i]));
+    int e = 0;
+    if (mx > 0.0) {
+        std::frexp(mx, &e);  // mx < 2^e
+        e += 2;              // |w| / 2^ew < 1/4
+    }
+    s.ew = e;
+    for (int i = 0; i < 49; ++i) {
+        double a = std::ldexp(w.v[i], kDigitBits - e);  // |a| < 128, exact
+        for (int k = 0; k < 6; ++k) {
+            const double d = std::rint(a);
+            s.d[k][i] = __float2half_rn((float)d);
+            a = (a - d) * 512.0;  // exact: a - d is a multiple of a's last bit
+        }
+    }
+    return s;
+}
+
+// ---- FP64 digits and recombination (integer operations only)
+
+// 256 in each of six 9-bit fields: Y = X + kF64Bias has fields u in [0, 511]
+// (top field up to 384) with X = sum (u_k - 256) 512^(5-k).
+constexpr unsigned long long kF64Bias = 256ull * ((1ull << 54) - 1) / 511;
+
+// Biased-digit word of one FP64 value (bits lo, hi) of a tile whose largest
+// biased exponent is eb1 (at least 1): X = round(x / 2^(eb1 - 1074)), so
+// |X| <= 2^52, returned as X + kF64Bias.
+__device__ __forceinline__ unsigned long long f64_biased_fixed(unsigned lo, unsigned hi, int eb1)
+{
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const int ee = max(e, 1);  // subnormals: no implicit bit, exponent 1
+    const unsigned long long mant =
+        ((unsigned long long)((hi & 0xFFFFFu) | (e ? 0x100000u : 0u)) << 32) | lo;
+    const int s = eb1 + 1 - ee;  // >= 1
+    const unsigned long long x = s < 56 ? ((mant >> (s - 1)) + 1) >> 1 : 0ull;  // round half up
+    return (hi >> 31) ? kF64Bias - x : kF64Bias + x;
+}
+
+// Digit k (0 = most significant) of two biased words, as an FP16 pair:
+// FP16 (1024 + u) has the bits 0x6400 | u, and (1024 + u) - 1280 = u - 256
+// is exact in FP16.
+template <int K>
+__device__ __forceinline__ unsigned f64_digit_pair(unsigned long long ya, unsigned long long yb)
+{
+    constexpr int sh = kDigitBits * (5 - K);
+    unsigned ua = (unsigned)(ya >> sh), ub = (unsigned)(yb >> sh);
+    if constexpr (K > 0) {
+        ua &= 511u;
+        ub &= 511u;
+    }
+    const unsigned w = (ua | (ub << 16)) | 0x64006400u;
+    const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&w), __halves2half2(__ushort_as_half(0x6500),
+                                                                                     __ushort_as_half(0x6500)));
+    return *reinterpret_cast<const unsigned *>(&h);
+}
+
+// FP64 value of T * 2^(be0 - 1086), rounded to nearest even, from integer
+// operations; results outside the normal range take the FP64 route.
+__device__ __forceinline__ double f64_from_fixed(long long t, int be0)
+{
+    if (t == 0) return 0.0;
+    const unsigned long long sign = (unsigned long long)t & 0x8000000000000000ull;
+    const unsigned long long a = t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
+    const int lz = __clzll((long long)a);
+    const unsigned long long an = a << lz;  // bit 63 set
+    const unsigned long long mant = an >> 11;
+    const unsigned rb = (unsigned)an & 0x7FFu;
+    const unsigned long long up = (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    const int be = be0 - lz;  // biased exponent of the result
+    if (be >= 1 && be <= 2046)
+        return __longlong_as_double((long long)(sign | ((((unsigned long long)(be - 1)) << 52) + mant + up)));
+    return scalbn((double)t, be0 - 1086);  // subnormal or overflowing results
+}
+
+// Marks a tile whose window holds an Inf or NaN (its outputs become NaN).
+constexpr int kNonFiniteTile = -100000;
 
 // Warp roles.
 constexpr int kSliceWarps = 8, kEpiWarps = 8;
@@ -84,17 +203,20 @@ constexpr int PL = ST_X * ST_Y;            // halves per digit plane (10,080 byt
 constexpr unsigned kRowBytes = ST_X * 2;   // 144
 constexpr int NOFF = R + 6;                // window row offsets per row group
 constexpr int NLV = 8 * R;                 // accumulator columns per level
-constexpr int NCOL = NLV * kDigits;        // 160: level L at NLV * L
 constexpr int kAccStride = 256;            // TMEM columns between the two accumulators
 constexpr int kTmemCols = 512;
-constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 40,320
+constexpr unsigned kStageBytes = ST_X * ST_Y * 8;  // 40,320 (8-byte points)
 constexpr int PAIRS = ST_X / 2, NPAIR = ST_Y * PAIRS;           // 36, 2,520
 constexpr int PER = (NPAIR + kSliceThreads - 1) / kSliceThreads;  // 10
 static_assert(kEpiWarps == 2 * 4 && R == 4, "two epilogue warps per TMEM lane quarter, two rows each");
 
+template <class F>
 struct Smem {
-    float2 stage[ST_Y * ST_X];                 // TMA destination
-    __half planes[2][kDigits][PL];             // digit planes, two tiles
+    static constexpr int D = F::kDigits;
+    static constexpr int NCOL = NLV * D;       // level L at NLV * L
+    static_assert(NCOL <= kAccStride, "an accumulator must fit between the two TMEM bases");
+    uint4 stage[NPAIR];                        // TMA destination: pairs of 8-byte points
+    __half planes[2][D][PL];                   // digit planes, two tiles
     __half bmat[NOFF][NCOL * 16];              // B_i, K-major 8x16-byte core matrices
     unsigned long long stage_full, stage_empty;
     unsigned long long planes_full[2], planes_empty[2];
@@ -103,46 +225,50 @@ struct Smem {
     int abort;                                 // set by the first expired wait
     int wait_ok[2];                            // slicer leader's wait results
     int scale_exp[4];                          // per-tile input scale, ring of 4
-    float red[kSliceWarps];
+    float red[kSliceWarps];                    // split: per-warp max |hi|
+    int redi[kSliceWarps];                     // FP64: per-warp max biased exponent
 };
 
-// The MMAs of one tile: window row offset I, input digit D. Descriptor
+static_assert(sizeof(Smem<FmtF64>) + 128 <= 232448 && sizeof(Smem<FmtSplit>) + 128 <= 232448,
+              "shared memory of one CTA must stay within 227 KB");
+
+// The MMAs of one tile: window row offset I, input digit DG. Descriptor
 // addresses advance in 16-byte units: digit planes are PL halves apart, row
 // offsets one plane row, B_i matrices NCOL * 16 halves.
-template <int I, int D>
+template <int D, int I, int DG>
 __device__ __forceinline__ void tile_mma(unsigned d_base, unsigned long long a0, unsigned long long b0)
 {
-    constexpr unsigned long long a_off = ((unsigned long long)D * PL * 2 + I * kRowBytes) >> 4;
+    constexpr int NCOL = NLV * D;
+    constexpr unsigned long long a_off = ((unsigned long long)DG * PL * 2 + I * kRowBytes) >> 4;
     constexpr unsigned long long b_off = ((unsigned long long)I * NCOL * 16 * 2) >> 4;
-    static_assert(((unsigned long long)D * PL * 2 + I * kRowBytes) % 16 == 0 && (NCOL * 16 * 2) % 16 == 0,
+    static_assert(((unsigned long long)DG * PL * 2 + I * kRowBytes) % 16 == 0 && (NCOL * 16 * 2) % 16 == 0,
                   "descriptor offsets must be 16-byte multiples");
-    mma_f16(d_base + (unsigned)(NLV * D), a0 + a_off, b0 + b_off, instr_desc(NLV * (kDigits - D)),
-            (I | D) != 0 ? 1u : 0u);
-    if constexpr (D + 1 < kDigits)
-        tile_mma<I, D + 1>(d_base, a0, b0);
+    mma_f16(d_base + (unsigned)(NLV * DG), a0 + a_off, b0 + b_off, instr_desc(NLV * (D - DG)),
+            (I | DG) != 0 ? 1u : 0u);
+    if constexpr (DG + 1 < D)
+        tile_mma<D, I, DG + 1>(d_base, a0, b0);
     else if constexpr (I + 1 < NOFF)
-        tile_mma<I + 1, 0>(d_base, a0, b0);
+        tile_mma<D, I + 1, 0>(d_base, a0, b0);
 }
 
-__device__ __forceinline__ void issue_tile_mmas(unsigned d_base, unsigned long long a0, unsigned long long b0)
-{
-    tile_mma<0, 0>(d_base, a0, b0);
-}
-
+template <class F>
 __global__ void __launch_bounds__(kThreads, 1)
-    k2d_tc(const __grid_constant__ CUtensorMap tmap, float2 *__restrict__ out, int m, int n,
-           long long ld, int tiles_x, int tiles, int map_x, int map_y, SliceWeights sw)
+    k2d_tc(const __grid_constant__ CUtensorMap tmap, typename F::Out *__restrict__ out, int m, int n,
+           long long ld, int tiles_x, int tiles, int map_x, int map_y, typename F::Digits sw, WaitCfg wc)
 {
+    constexpr int D = F::kDigits;
+    constexpr int NCOL = NLV * D;
+    using SM = Smem<F>;
     extern __shared__ unsigned char smem_raw[];
-    Smem &S = *reinterpret_cast<Smem *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    SM &S = *reinterpret_cast<SM *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int my_tiles = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     volatile int *abort = &S.abort;
     const unsigned stage_full = smem_addr(&S.stage_full), stage_empty = smem_addr(&S.stage_empty);
     auto bar2 = [](unsigned long long (&b)[2], int i) { return smem_addr(&b[i]); };
-    auto wait = [abort](unsigned bar, unsigned parity) {
-        return mbar_wait(bar, parity, abort, &g_tc_wait_timeouts);
+    const unsigned long long limit = wc.limit_ns;
+    auto wait = [abort, limit](unsigned bar, unsigned parity) {
+        return mbar_wait(bar, parity, abort, &g_tc_wait_timeouts, limit);
     };
 
     int issued = 0, committed = 0;  // window loads issued / MMA batches committed (one thread each)
@@ -157,12 +283,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if (my_tiles > 0) {  // the first window load overlaps the set-up below
+        if (my_tiles > 0 && !wc.skip_loads) {  // the first window load overlaps the set-up below
             const int ty = (int)blockIdx.x / tiles_x;
             const int x0 = ((int)blockIdx.x - ty * tiles_x) * TX, y0 = ty * TY;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(stage_full),
-                         "r"(kStageBytes)
-                         : "memory");
+            mbar_expect_tx(stage_full, kStageBytes);
             tma_load_2d(smem_addr(S.stage), &tmap, map_x + x0 - 4, map_y + y0 - 3, stage_full);
             issued = 1;
         }
@@ -197,15 +321,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
-        if (lane == 0) {
+        if (lane == 0 && !wc.skip_loads) {
             for (int it = issued; it < my_tiles; ++it) {
                 if (!wait(stage_empty, (it & 1) ^ 1)) break;
                 int x0, y0;
                 tile_origin(it, x0, y0);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(stage_full),
-                             "r"(kStageBytes)
-                             : "memory");
+                mbar_expect_tx(stage_full, kStageBytes);
                 tma_load_2d(smem_addr(S.stage), &tmap, map_x + x0 - 4, map_y + y0 - 3, stage_full);
                 issued = it + 1;
             }
@@ -222,9 +344,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (!wait(bar2(S.acc_empty, buf), (use & 1) ^ 1)) break;
                 tc_fence_after();
                 // The issuing thread stalls on every MMA until the tensor core
-                // takes it, so nothing else sits between them: all 50 are
+                // takes it, so nothing else sits between them: all MMAs are
                 // unrolled, each descriptor one add of a compile-time offset.
-                issue_tile_mmas(tmem + (unsigned)(kAccStride * buf), buf ? a_desc_buf1 : a_desc_buf0, b_desc0);
+                tile_mma<D, 0, 0>(tmem + (unsigned)(kAccStride * buf), buf ? a_desc_buf1 : a_desc_buf0, b_desc0);
                 mma_commit(bar2(S.planes_empty, buf));  // planes may be overwritten
                 mma_commit(bar2(S.acc_full, buf));      // accumulator ready
                 committed = it + 1;
@@ -241,48 +363,85 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("bar.sync %0, %1;" ::"n"(kSliceBarrier), "n"(kSliceThreads) : "memory");
             if (!S.wait_ok[0]) break;
             // (b) window -> registers, then release the stage to the next load.
-            const float4 *stg = reinterpret_cast<const float4 *>(S.stage);
-            float4 v[PER];
-            float vmax = 0.f;
+            uint4 v[PER];
+            float vmax = 0.f;   // split: largest |hi|
+            unsigned emax = 0;  // FP64: largest biased exponent
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
                 const int idx = st + q * kSliceThreads;
-                v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                v[q] = make_uint4(0u, 0u, 0u, 0u);
                 if (idx < NPAIR) {
-                    v[q] = stg[idx];
-                    vmax = fmaxf(vmax, fmaxf(fabsf(v[q].x), fabsf(v[q].z)));
+                    v[q] = S.stage[idx];
+                    if constexpr (F::kF64)
+                        emax = max(emax, max((v[q].y >> 20) & 0x7FFu, (v[q].w >> 20) & 0x7FFu));
+                    else
+                        vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(v[q].x)), fabsf(__uint_as_float(v[q].z))));
                 }
             }
+            if constexpr (F::kF64) {
+                emax = __reduce_max_sync(0xffffffffu, emax);
+            } else {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+                for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+            }
             __syncwarp();
             if (lane == 0) {
-                S.red[warp - kWarpSlice0] = vmax;
+                if constexpr (F::kF64)
+                    S.redi[warp - kWarpSlice0] = (int)emax;
+                else
+                    S.red[warp - kWarpSlice0] = vmax;
                 mbar_arrive(stage_empty);
             }
             // (c) planes of this buffer free (MMAs two tiles back done)?
             if (leader) S.wait_ok[1] = wait(bar2(S.planes_empty, buf), (use & 1) ^ 1);
             asm volatile("bar.sync %0, %1;" ::"n"(kSliceBarrier), "n"(kSliceThreads) : "memory");
             const bool go = S.wait_ok[1];
-            vmax = S.red[0];
+            int ex;
+            if constexpr (F::kF64) {
+                int eb = S.redi[0];
 #pragma unroll
-            for (int i = 1; i < kSliceWarps; ++i) vmax = fmaxf(vmax, S.red[i]);
-            // (d) every slicer has read wait_ok[1] and red[] before they are reused
+                for (int i = 1; i < kSliceWarps; ++i) eb = max(eb, S.redi[i]);
+                ex = max(eb, 1);
+            } else {
+                vmax = S.red[0];
+#pragma unroll
+                for (int i = 1; i < kSliceWarps; ++i) vmax = fmaxf(vmax, S.red[i]);
+                ex = split::tile_exponent(vmax);
+            }
+            // (d) every slicer has read wait_ok[1] and the maxima before they are reused
             asm volatile("bar.sync %0, %1;" ::"n"(kSliceBarrier), "n"(kSliceThreads) : "memory");
             if (!go) break;
-            const int ex = split::tile_exponent(vmax);
-            if (leader) S.scale_exp[it & 3] = ex;
-            const float to_digits = ldexpf(1.0f, kDigitBits - ex);
+            if (leader) S.scale_exp[it & 3] = (F::kF64 && ex == 2047) ? kNonFiniteTile : ex;
+            unsigned *dst0 = reinterpret_cast<unsigned *>(&S.planes[buf][0][0]);
+            if constexpr (F::kF64) {
 #pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int idx = st + q * kSliceThreads;
-                if (idx < NPAIR) {
-                    float d0[kDigits], d1[kDigits];
-                    slice_digits(v[q].x * to_digits, v[q].y * to_digits, d0);
-                    slice_digits(v[q].z * to_digits, v[q].w * to_digits, d1);
-                    unsigned *dst = reinterpret_cast<unsigned *>(&S.planes[buf][0][0]) + idx;
+                for (int q = 0; q < PER; ++q) {
+                    const int idx = st + q * kSliceThreads;
+                    if (idx < NPAIR) {
+                        const unsigned long long ya = f64_biased_fixed(v[q].x, v[q].y, ex);
+                        const unsigned long long yb = f64_biased_fixed(v[q].z, v[q].w, ex);
+                        unsigned *dst = dst0 + idx;
+                        dst[0 * (PL / 2)] = f64_digit_pair<0>(ya, yb);
+                        dst[1 * (PL / 2)] = f64_digit_pair<1>(ya, yb);
+                        dst[2 * (PL / 2)] = f64_digit_pair<2>(ya, yb);
+                        dst[3 * (PL / 2)] = f64_digit_pair<3>(ya, yb);
+                        dst[4 * (PL / 2)] = f64_digit_pair<4>(ya, yb);
+                        dst[5 * (PL / 2)] = f64_digit_pair<5>(ya, yb);
+                    }
+                }
+            } else {
+                const float to_digits = ldexpf(1.0f, kDigitBits - ex);
 #pragma unroll
-                    for (int k = 0; k < kDigits; ++k) dst[k * (PL / 2)] = split::pack_h2(d0[k], d1[k]);
+                for (int q = 0; q < PER; ++q) {
+                    const int idx = st + q * kSliceThreads;
+                    if (idx < NPAIR) {
+                        float d0[D], d1[D];
+                        slice_digits(__uint_as_float(v[q].x) * to_digits, __uint_as_float(v[q].y) * to_digits, d0);
+                        slice_digits(__uint_as_float(v[q].z) * to_digits, __uint_as_float(v[q].w) * to_digits, d1);
+                        unsigned *dst = dst0 + idx;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) dst[k * (PL / 2)] = split::pack_h2(d0[k], d1[k]);
+                    }
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -304,14 +463,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc_fence_after();
             int x0, y0;
             tile_origin(it, x0, y0);
-            const float scale = ldexpf(1.0f, S.scale_exp[it & 3] + sw.ew - 2 * kDigitBits);
+            const int ex = S.scale_exp[it & 3];
             const int xb = x0 + 8 * eb;
 #pragma unroll 1
             for (int pass = 0; pass < 2; ++pass) {
                 const int rho = 2 * h + pass;
-                float acc[kDigits][8];
+                float acc[D][8];
 #pragma unroll
-                for (int L = 0; L < kDigits; ++L)
+                for (int L = 0; L < D; ++L)
                     tmem_ld8(tmem + lane_bits + (unsigned)(kAccStride * buf + NLV * L + 8 * rho), acc[L]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (pass == 1) {  // accumulator drained: hand it back to the MMA warp
@@ -320,7 +479,33 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (lane == 0) mbar_arrive(bar2(S.acc_empty, buf));
                 }
                 const int yy = y0 + R * er + rho;
-                if (yy < m) {
+                if (yy >= m) continue;
+                if constexpr (F::kF64) {
+                    // T = sum over levels of S_L 2^(42 - 9L) (level 5 without
+                    // its last three bits): |T| < 2^63; value T 2^(be0 - 1086).
+                    const int be0 = ex + sw.ew + 6;
+                    double res[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const long long t = ((long long)__float2int_rn(acc[0][j]) << 42) +
+                                            ((long long)__float2int_rn(acc[1][j]) << 33) +
+                                            ((long long)__float2int_rn(acc[2][j]) << 24) +
+                                            ((long long)__float2int_rn(acc[3][j]) << 15) +
+                                            ((long long)__float2int_rn(acc[4][j]) << 6) +
+                                            (long long)(__float2int_rn(acc[5][j]) >> 3);
+                        res[j] = ex == kNonFiniteTile ? __longlong_as_double(0x7FF8000000000000ll)
+                                                      : f64_from_fixed(t, be0);
+                    }
+                    double *o = reinterpret_cast<double *>(out) + (long long)yy * ld + xb;
+#pragma unroll
+                    for (int j = 0; j < 8; j += 2) {
+                        if (xb + j + 1 < n)
+                            *reinterpret_cast<double2 *>(o + j) = make_double2(res[j], res[j + 1]);
+                        else if (xb + j < n)
+                            o[j] = res[j];
+                    }
+                } else {
+                    const float scale = ldexpf(1.0f, ex + sw.ew - 2 * kDigitBits);
                     float2 res[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
@@ -331,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         two_sum(h2, (e1 + e2) + tail, hi, lo);
                         res[j] = make_float2(hi * scale, lo * scale);
                     }
-                    float2 *o = out + (long long)yy * ld + xb;
+                    float2 *o = reinterpret_cast<float2 *>(out) + (long long)yy * ld + xb;
 #pragma unroll
                     for (int j = 0; j < 8; j += 2) {
                         if (xb + j + 1 < n)
@@ -360,21 +545,21 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-}  // namespace
-
-cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long origin,
-                                  long long elements, const float2 *in_base, float2 *out_base,
-                                  cudaStream_t st)
+template <class F>
+cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long long origin, long long elements,
+                      const void *in_base, void *out_base, const WaitCfg &wc, cudaStream_t st)
 {
     const long long ld = g.pitch[0];
     CUtensorMap map;
-    cudaError_t e = encode_split_window_map(&map, in_base, ld, elements / ld, ST_X, ST_Y);
+    // The map copies 8-byte points whatever they hold ((hi, lo) pairs or FP64).
+    cudaError_t e = encode_split_window_map(&map, reinterpret_cast<const float2 *>(in_base), ld, elements / ld,
+                                            ST_X, ST_Y);
     if (e != cudaSuccess) return e;
-    const size_t smem = sizeof(Smem) + 128;
+    const size_t smem = sizeof(Smem<F>) + 128;
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(attr_once, [smem] {
-        attr_err = cudaFuncSetAttribute(k2d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_err = cudaFuncSetAttribute(k2d_tc<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
     if (attr_err != cudaSuccess) return attr_err;
     const int tiles_x = (int)((g.ext[1] + TX - 1) / TX);
@@ -383,10 +568,27 @@ cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long
     // the TMEM allocation never waits).
     const int grid = std::min(tiles, device_sm_count());
     note_launch();
-    k2d_tc<<<grid, kThreads, smem, st>>>(map, out_base + origin, (int)g.ext[0], (int)g.ext[1], ld,
-                                        tiles_x, tiles, (int)(origin % ld), (int)(origin / ld),
-                                        split::slice_weights(w));
+    k2d_tc<F><<<grid, kThreads, smem, st>>>(map, reinterpret_cast<typename F::Out *>(out_base) + origin,
+                                            (int)g.ext[0], (int)g.ext[1], ld, tiles_x, tiles, (int)(origin % ld),
+                                            (int)(origin / ld), digits, wc);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long origin,
+                                  long long elements, const float2 *in_base, float2 *out_base,
+                                  const TcWait &wt, cudaStream_t st)
+{
+    return launch_tc<FmtSplit>(g, split::slice_weights(w), origin, elements, in_base, out_base,
+                               WaitCfg{wt.limit_ns, wt.skip_loads}, st);
+}
+
+cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long origin, long long elements,
+                                 const double *in_base, double *out_base, const TcWait &wt, cudaStream_t st)
+{
+    return launch_tc<FmtF64>(g, f64_slice_weights(w), origin, elements, in_base, out_base,
+                             WaitCfg{wt.limit_ns, wt.skip_loads}, st);
 }
 
 cudaError_t split_tc_wait_timeouts(unsigned *count, bool reset)

@@ -40,7 +40,7 @@
 //     recombine each plane's levels, add the three double-float partial sums
 //     of an output relative to the largest plane scale, scale once and store.
 //
-// Every mbarrier wait is bounded (2 s of %globaltimer). An expired wait is
+// Every mbarrier wait is bounded (WaitCfg, 2 s by default). An expired wait is
 // counted in g_tc3d_wait_timeouts; the CTA then waits, again bounded, for the
 // TMA copies and the MMAs it still has in flight, frees its TMEM and leaves.
 #include "cs_internal.h"
@@ -167,7 +167,7 @@ __device__ __forceinline__ void recombine(const float (&acc)[kDigits], float &hi
 __global__ void __launch_bounds__(kThreads, 1)
     k3d_tc(const __grid_constant__ CUtensorMap tmap, float2 *__restrict__ out, int h, int m, int n,
            long long ldy, long long ldz, int tiles_x, int tiles_y, int zc, int items, int map_x, int map_y,
-           int map_z, SliceWeights sw)
+           int map_z, SliceWeights sw, WaitCfg wc)
 {
     extern __shared__ unsigned char smem_raw[];
     Smem &S = *reinterpret_cast<Smem *>(
@@ -175,8 +175,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     volatile int *abort = &S.abort;
     auto bar = [](unsigned long long *b, int i) { return smem_addr(&b[i]); };
-    auto wait = [abort](unsigned b, unsigned parity) {
-        return mbar_wait(b, parity, abort, &g_tc3d_wait_timeouts);
+    const unsigned long long limit = wc.limit_ns;
+    auto wait = [abort, limit](unsigned b, unsigned parity) {
+        return mbar_wait(b, parity, abort, &g_tc3d_wait_timeouts, limit);
     };
     const int first = blockIdx.x, step = gridDim.x;
 
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
-        if (lane == 0) {
+        if (lane == 0 && !wc.skip_loads) {
             int q = 0;  // input-plane sequence number
             bool ok = true;
             for (int item = first; item < items && ok; item += step) {
@@ -465,7 +466,7 @@ bool split_tc3d_layout_ok(const GridView &g, long long origin, const void *in_ba
 
 cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
                                     long long elements, const float2 *in_base, float2 *out_base,
-                                    cudaStream_t st)
+                                    const TcWait &wt, cudaStream_t st)
 {
     const long long ldy = g.pitch[1], ldz = g.pitch[0];
     CUtensorMap map;
@@ -497,7 +498,8 @@ cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long lo
     note_launch();
     k3d_tc<<<grid, kThreads, smem, st>>>(map, out_base + origin, h, m, n, ldy, ldz, tiles_x, tiles_y, zc,
                                         items, (int)(origin % ldy), (int)((origin % ldz) / ldy),
-                                        (int)(origin / ldz), split::slice_weights(w, 27));
+                                        (int)(origin / ldz), split::slice_weights(w, 27),
+                                        WaitCfg{wt.limit_ns, wt.skip_loads});
     return cudaGetLastError();
 }
 

@@ -9,6 +9,8 @@
 #include "../../include/convstencil.h"
 #include "cs_internal.h"
 
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 
@@ -28,7 +30,31 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void *g_addr[kMaxDevices];  // device address of the scratch, per device
+// Device address of the scratch, per device, with the driver context it was
+// looked up in: after cudaDeviceReset (or under another context) the module
+// is loaded again, possibly at another address, so a changed context repeats
+// the look-up.
+void *g_addr[kMaxDevices];
+CUcontext g_ctx[kMaxDevices];
+
+// The current driver context (null if none or unknown), through the runtime's
+// driver entry point so that the library needs no link-time libcuda symbol.
+CUcontext current_context()
+{
+    typedef CUresult (*CtxGetCurrent)(CUcontext *);
+    static CtxGetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrent>(p);
+    });
+    CUcontext ctx = nullptr;
+    if (!fn || fn(&ctx) != CUDA_SUCCESS) return nullptr;
+    return ctx;
+}
 
 }  // namespace
 
@@ -50,22 +76,34 @@ extern "C" CS_API cs_status cs_run_noalloc(cs_plan *plan, const void *in, void *
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cs::set_error(CS_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return cs::set_error(CS_ERR_UNSUPPORTED, "device index out of range");
+    // Rejected calls leave the shared scratch untouched: the step count is
+    // checked before anything is queued.
+    long long sweeps = 0;
+    const cs_status ss = cs_plan_sweeps(plan, steps, &sweeps);
+    if (ss != CS_OK) return ss;
     void *scratch = nullptr;
     {
-        // Once per device, with that device current: the host-side name of a
-        // __device__ array is not a device address, so ask the runtime for it.
+        // Once per device (and driver context), with that device current: the
+        // host-side name of a __device__ array is not a device address, so
+        // ask the runtime for it.
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
+        CUcontext ctx = current_context();
+        if (!g_addr[dev] || g_ctx[dev] != ctx) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) return cs::set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+            ctx = current_context();  // the look-up may have made the primary context current
             g_addr[dev] = p;
+            g_ctx[dev] = ctx;
         }
         scratch = g_addr[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    // The scratch keeps whatever the previous call left; its halo must read as zero.
-    e = cudaMemsetAsync(scratch, 0, bytes, st);
-    if (e != cudaSuccess) return cs::set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+    // The scratch keeps whatever the previous call left; its halo must read
+    // as zero. A zero-sweep call only copies `in` to `out` and never reads it.
+    if (sweeps > 0) {
+        e = cudaMemsetAsync(scratch, 0, bytes, st);
+        if (e != cudaSuccess) return cs::set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+    }
     return cs::run_into(plan, in, out, scratch, steps, st);
 }

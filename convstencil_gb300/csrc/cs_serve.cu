@@ -12,7 +12,12 @@
 //     issued whole, chunk after chunk, on high-priority streams, so the
 //     hardware runs their kernels ahead of the large requests' chunks;
 //   * completion: the result goes to a pinned host buffer, the device memory is
-//     released (making room for queued requests), the latency is recorded.
+//     released (making room for queued requests), the latency is recorded. A
+//     request during whose life a bounded device-side wait expired (the
+//     library's wait-timeout counters moved between its admission and its
+//     completion) is reported as CS_ERR_TIMEOUT instead: its result may be
+//     incomplete. The attribution is conservative: a request that overlapped
+//     another's expiry is reported too.
 // Kernel choice and FP64 re-anchoring points depend only on the request, never
 // on what else is running, so a request's result is bitwise identical alone
 // and in any mix.
@@ -105,6 +110,7 @@ struct Request {
     long long graph_steps = 0;
     int full_chunks = 0;
     double t_submit = 0, t_done = 0;
+    unsigned waits_at_start = 0;  // wait-timeout count when admitted
     std::atomic<State> state{State::Queued};
     bool retired = false;
     cs_status status = CS_OK;
@@ -162,6 +168,7 @@ void release_device(Request *r)
 bool start_request(cs_server *s, Request *r)
 {
     const size_t b = r->layout.bytes;
+    cs_device_wait_timeouts(&r->waits_at_start, 0);
     r->stream = r->small ? s->fast_streams[s->rr_fast++ % s->fast_streams.size()]
                          : s->streams[s->rr++ % s->streams.size()];
     cudaError_t e = cudaSuccess;
@@ -339,7 +346,16 @@ void worker_main(cs_server *s)
                 advance(s, r);
                 progressed |= r->issued != before;
             }
-            const bool finished = r->state == State::Draining && cudaEventQuery(r->done_ev) == cudaSuccess;
+            bool finished = r->state == State::Draining && cudaEventQuery(r->done_ev) == cudaSuccess;
+            if (finished) {
+                unsigned waits = 0;
+                if (cs_device_wait_timeouts(&waits, 0) == CS_OK && waits != r->waits_at_start) {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    fail_request(s, r, CS_ERR_TIMEOUT,
+                                 "a bounded device-side wait expired while this request ran; result incomplete");
+                    finished = false;
+                }
+            }
             if (finished || r->state == State::Failed) {
                 std::lock_guard<std::mutex> lk(s->mu);
                 if (finished) {
@@ -468,7 +484,16 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
                                                                                  : 2;
         cs_plan_set_option(r->plan, CS_OPT_TIME_BLOCK, tb);
     } else {
-        cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_FMA);
+        // FP64: 7x7 kernels of at least four 64 x 64 tiles per SM on the
+        // tcgen05 digit pipeline (same cost model as the split slices), the
+        // FP64 FMA kernels otherwise.
+        const long long tiles = ((d->extent[0] + 63) / 64) * ((d->extent[1] + 63) / 64);
+        const bool r3_2d = (d->shape == CS_SHAPE_BOX2D3R || d->shape == CS_SHAPE_STAR2D3R ||
+                            (d->semantics == CS_SEM_FUSED &&
+                             (d->shape == CS_SHAPE_BOX2D1R || d->shape == CS_SHAPE_STAR2D1R)));
+        if (!(r3_2d && tiles >= 4LL * s->sm_count &&
+              cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_TC) == CS_OK))
+            cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_FMA);
     }
     cs_plan_set_option(r->plan, CS_OPT_REANCHOR_INTERVAL, 0);  // the server re-anchors at global steps
     long long sweeps1 = 0;

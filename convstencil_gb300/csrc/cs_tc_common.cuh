@@ -3,10 +3,12 @@
 // mbarrier waits, shared-memory matrix and instruction descriptors for
 // kind::f16 MMAs with TMEM accumulators, TMEM loads and TMA tile loads.
 //
-// Every wait is bounded by kWaitNs of %globaltimer. An expired wait adds one
-// to the caller's device counter and raises the CTA's abort flag, so every
-// role of the CTA stops at its next wait; mbar_drain is the bounded wait used
-// at exit for copies and MMAs still in flight.
+// Every wait is bounded by WaitCfg::limit_ns of %globaltimer (2 s unless the
+// plan sets another limit). An expired wait adds one to the caller's device
+// counter and raises the CTA's abort flag, so every role of the CTA stops at
+// its next wait; mbar_drain is the bounded wait used at exit for copies and
+// MMAs still in flight. The host reads the counter after synchronous runs and
+// reports CS_ERR_TIMEOUT.
 #pragma once
 
 #include <cuda.h>
@@ -15,7 +17,14 @@
 namespace cs {
 namespace tc {
 
-constexpr unsigned long long kWaitNs = 2000000000ull;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // default bound of one wait
+
+// Per-launch wait settings (kernel parameter).
+struct WaitCfg {
+    unsigned long long limit_ns;  // bound of every mbarrier wait
+    int skip_loads;               // test hook: the producer issues no TMA loads, so the
+                                  // consumers' first wait runs out and the CTA leaves
+};
 
 __device__ __forceinline__ unsigned smem_addr(const void *p)
 {
@@ -41,11 +50,11 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
     return ok != 0;
 }
 
-// Waits for the phase with the given parity. Gives up after kWaitNs (counted
-// in *timeouts, and *abort raised so every other role stops too) or as soon
-// as another role has raised *abort.
+// Waits for the phase with the given parity. Gives up after limit_ns
+// (counted in *timeouts, and *abort raised so every other role stops too) or
+// as soon as another role has raised *abort.
 static __device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity, volatile int *abort,
-                                              unsigned *timeouts)
+                                              unsigned *timeouts, unsigned long long limit_ns = kWaitNs)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = globaltimer();
@@ -53,7 +62,7 @@ static __device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity, vol
         for (int i = 0; i < 16; ++i)
             if (mbar_try_wait(bar, parity)) return true;
         if (*abort) return false;
-        if (globaltimer() - t0 > kWaitNs) {
+        if (globaltimer() - t0 > limit_ns) {
             atomicAdd(timeouts, 1u);
             *abort = 1;
             return false;
@@ -62,11 +71,12 @@ static __device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity, vol
 }
 
 // Bounded wait used only at exit for copies / MMAs still in flight.
-static __device__ __noinline__ bool mbar_drain(unsigned bar, unsigned parity, unsigned *timeouts)
+static __device__ __noinline__ bool mbar_drain(unsigned bar, unsigned parity, unsigned *timeouts,
+                                               unsigned long long limit_ns = kWaitNs)
 {
     const unsigned long long t0 = globaltimer();
     while (!mbar_try_wait(bar, parity))
-        if (globaltimer() - t0 > kWaitNs) {
+        if (globaltimer() - t0 > limit_ns) {
             atomicAdd(timeouts, 1u);
             return false;
         }

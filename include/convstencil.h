@@ -65,10 +65,16 @@ typedef enum cs_shape {
 typedef enum cs_semantics { CS_SEM_STEP = 0, CS_SEM_FUSED = 1 } cs_semantics;
 
 /* Arithmetic of the sweep.
- * CS_PREC_FP64 : FP64 grids, FP64 arithmetic (FP64 FMA or FP64 MMA).
+ * CS_PREC_FP64 : FP64 grids. FP64 FMA or FP64 MMA arithmetic, or, for 2D
+ *                dense 7x7 kernels, the FP64-accurate tensor-core form
+ *                (CS_ALGO_FP64_TC) when the tuner measures it faster: every
+ *                product and level sum is exact, inputs keep 52 bits below
+ *                their 64x70 tile's largest value and weights 53 below the
+ *                largest weight (relative error per sweep ~1e-16 of the
+ *                tile's scale). Pin CS_ALGO_FP64_FMA for IEEE FP64 sums.
  * CS_PREC_SPLIT: grids stored as FP32 (hi, lo) pairs (8 bytes per point,
  *                about 48 significant bits); no FP64 arithmetic in the sweep.
- *                Dense 7x7 kernels contract exact 10-bit fixed-point slices
+ *                Dense 7x7 kernels contract exact 9-bit fixed-point slices
  *                on FP16 tensor cores (FP32 accumulation is exact for them);
  *                other kernels use double-float FP32 arithmetic. Relative
  *                error per sweep ~1e-13. Inputs must be finite. */
@@ -86,18 +92,31 @@ typedef enum cs_algo {
     CS_ALGO_SPLIT_FMA = 4, /* split precision: double-float arithmetic on FP32 cores */
     CS_ALGO_SPLIT_MMA_TMA = 5, /* as CS_ALGO_SPLIT_MMA, tiles fetched by TMA (cp.async.bulk.tensor)
                                   one tile ahead */
-    CS_ALGO_SPLIT_TC = 6 /* the same slices on fifth-generation tensor cores (tcgen05.mma,
-                            accumulators in tensor memory), TMA-fed; 2D dense radius-3 kernels
-                            on buffers with an even pitch, >= 4 halo columns, 16-byte aligned */
+    CS_ALGO_SPLIT_TC = 6, /* the same slices on fifth-generation tensor cores (tcgen05.mma,
+                             accumulators in tensor memory), TMA-fed; 2D dense radius-3 kernels
+                             on buffers with an even pitch, >= 4 halo columns, 16-byte aligned;
+                             also 3D dense radius-1 split plans */
+    CS_ALGO_FP64_TC = 7   /* FP64 plans on the same tcgen05 pipeline: six exact 9-bit digits per
+                             operand cut from the FP64 bits by integer operations, exact FP32
+                             level sums, integer recombination to FP64 (no FP64 instruction in
+                             the sweep); 2D dense radius-3 FP64 plans of at least 8x8, same
+                             buffer conditions as CS_ALGO_SPLIT_TC */
 } cs_algo;
 
 typedef enum cs_option {
     CS_OPT_ALGO = 0,              /* cs_algo */
     CS_OPT_REANCHOR_INTERVAL = 2, /* split: renormalise (hi,lo) through FP64 every N
                                      sweeps (default 100, 0 = never) */
-    CS_OPT_TIME_BLOCK = 3         /* split double-float kernels, 2D radius 1 and 1D:
+    CS_OPT_TIME_BLOCK = 3,        /* split double-float kernels, 2D radius 1 and 1D:
                                      steps fused per launch by temporal blocking
                                      (0 = tuner picks 1..4, default; 1 = off) */
+    CS_OPT_WAIT_LIMIT_US = 4,     /* bound of each device-side wait of the tcgen05 kernels, in
+                                     microseconds (default 2,000,000; 1 .. 60,000,000) */
+    CS_OPT_WAIT_TEST_SKIP_LOADS = 5 /* test hook (0/1): the tcgen05 kernels issue no TMA loads,
+                                     so their first wait runs out after CS_OPT_WAIT_LIMIT_US and
+                                     the synchronous runs return CS_ERR_TIMEOUT; exercises the
+                                     timeout path without faulting the GPU. Outputs of such runs
+                                     are incomplete. */
 } cs_option;
 
 /* Where a grid lives in a buffer. extent/pitch are slowest axis first; the
@@ -156,11 +175,14 @@ CS_API cs_status cs_run(cs_plan *plan, void *a, void *b, long long steps, void *
  * Limits: one buffer of the plan's layout must fit in 16 MiB (2,097,152
  * points of 8 bytes); larger grids get CS_ERR_INVALID_ARGUMENT. The first
  * call on each device looks up the array's device address (with that device
- * current); make that first call before any stream capture. Every call shares
- * the one array per device: calls whose work overlaps on the GPU (different
- * streams, or threads) race on it and must be serialised by the caller.
- * With CS_ALGO_AUTO it uses the kernel the tuner already chose for this kind
- * of plan (else the default), and runs no tuning sweeps of its own. */
+ * current; again after the device's context changes, e.g. after
+ * cudaDeviceReset); make that first call before any stream capture. Every
+ * call shares the one array per device: calls whose work overlaps on the GPU
+ * (different streams, or threads) race on it and must be serialised by the
+ * caller. With CS_ALGO_AUTO it uses the kernel the tuner already chose for
+ * this kind of plan (else the default), and runs no tuning sweeps of its own.
+ * It launches one kernel per sweep, without cs_run's temporal blocking or
+ * CUDA-graph replay, so small grids run slower than through cs_run. */
 CS_API cs_status cs_run_noalloc(cs_plan *plan, const void *in, void *out, long long steps,
                                 void *stream);
 
@@ -170,11 +192,15 @@ CS_API cs_status cs_split_to_fp64(const cs_plan *plan, const void *src, double *
 
 /* Host-buffer form of cs_run: allocates two device grids, copies host_in
  * (FP64, plan layout) in, runs, copies the result (FP64) to host_out,
- * releases everything. Synchronous. */
+ * releases everything. Synchronous. Returns CS_ERR_TIMEOUT (result
+ * incomplete) if a bounded device-side wait expired during the call. */
 CS_API cs_status cs_run_host(cs_plan *plan, const double *host_in, double *host_out,
                              long long steps);
 
 /* ---- reference-shaped wrappers (FUSED semantics, reference layouts) ---- */
+/* Each returns CS_ERR_TIMEOUT (result incomplete) if a bounded device-side
+ * wait expired during the call; the reference exits on any CUDA error
+ * (src/2d/2d_utils.h:35-65). */
 /* Replaces gpu_1d1r (src/1d/1d_utils.h:75, src/1d/gpu_1r.cu:227-302).
  * in: n+7 doubles (index 0 alignment pad, halo 3); out: n+6 doubles, the
  * device array from index 1 (src/1d/gpu_1r.cu:299). params: 7. */

@@ -1,5 +1,6 @@
-"""Parity at the BASELINE configurations' full sizes, through properties that
-hold at any size (the CPU oracle would need hours at these sizes):
+"""Properties at the benchmark configurations' full sizes, beside the direct
+comparison with the CPU oracle in test_fullsize_oracle_gpu.py; they hold at
+any size and step count:
 
 * a constant field under weights summing to 1 stays constant wherever the
   zero halo has not reached yet (exactly, up to FP64 rounding);

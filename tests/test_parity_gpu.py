@@ -52,7 +52,7 @@ def test_golden_1d_step_plans(name):
 
 
 @pytest.mark.parametrize("name", G.names("g2d_"))
-@pytest.mark.parametrize("algo", [cs.Algo.FP64_FMA, cs.Algo.FP64_MMA])
+@pytest.mark.parametrize("algo", [cs.Algo.FP64_FMA, cs.Algo.FP64_MMA, cs.Algo.FP64_TC])
 def test_golden_2d(name, algo):
     c = G.load(name)
     m, n, T = int(c["m"]), int(c["n"]), int(c["sweeps"])
@@ -69,8 +69,9 @@ def test_golden_2d(name, algo):
     try:
         p.set_option(cs.Option.ALGO, algo)
     except cs.ConvStencilError as e:
-        assert e.status == 2 and algo == cs.Algo.FP64_MMA
-        pytest.skip("FP64 MMA serves dense radius-3 kernels only")
+        assert e.status == 2 and algo in (cs.Algo.FP64_MMA, cs.Algo.FP64_TC)
+        pytest.skip("FP64 MMA serves dense radius-3 kernels only; FP64 tcgen05 also needs >= 8x8 and an "
+                    "even row pitch")
     out = p.run_host(c["input"], T)
     assert rel_err(out, c["output"].reshape(-1))[0] <= TOL
 

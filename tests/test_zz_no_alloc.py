@@ -100,3 +100,51 @@ def test_noalloc_split_precision_and_size_limit():
     dummy2 = torch.zeros_like(dummy)
     assert _run_noalloc(big, dummy, dummy2, 1, None) == 1
     assert b"16777216" in cs.lib().cs_last_error()
+
+
+def _split_state(plan, x):
+    raw = torch.from_numpy(plan.pack(x)).cuda()
+    s = torch.zeros(plan.elements * 2, dtype=torch.float32, device="cuda")
+    plan.split_from_fp64(raw, s)
+    torch.cuda.synchronize()
+    return s
+
+
+def _to_fp64(plan, s):
+    r = torch.zeros(plan.elements, dtype=torch.float64, device="cuda")
+    plan.split_to_fp64(s, r)
+    torch.cuda.synchronize()
+    return plan.unpack(r.cpu().numpy())
+
+
+def test_noalloc_3d_tcgen05_zero_steps_and_fused_plan():
+    """The scratch array as the TMA source and destination of the 3D tcgen05
+    kernel, a zero-step call (out = in, scratch unused), and a fused 2D plan,
+    each against cs_run."""
+    cs.build()
+    ext = (40, 40, 40)
+    p3 = cs.Plan("box3d1r", ext, O.seeded_weights(27, 21), precision=cs.Precision.SPLIT)
+    p3.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    inp = _split_state(p3, O.splitmix_uniform(40 ** 3, 22).reshape(ext))
+    for steps in (4, 3):  # two calls in a row
+        want = _reference_run(p3, inp, steps)
+        out = torch.zeros_like(inp)
+        assert _run_noalloc(p3, inp, out, steps, None) == 0, cs.lib().cs_last_error()
+        torch.cuda.synchronize()
+        assert rel_err(_to_fp64(p3, out), _to_fp64(p3, want))[0] <= 1e-12
+    assert cs.device_wait_timeouts() == 0
+    out = torch.full_like(inp, 7.0)
+    assert _run_noalloc(p3, inp, out, 0, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(out, inp)
+    # fused box2d1r (3 steps per sweep): 6 steps = 2 sweeps; 4 steps is refused
+    w9 = O.seeded_weights(9, 23)
+    fused = O.selfconv(w9, 2, 1, 3)
+    pf = cs.Plan("box2d1r", (96, 130), fused, semantics=cs.Semantics.FUSED)
+    x = torch.from_numpy(pf.pack(O.splitmix_uniform(96 * 130, 24).reshape(96, 130))).cuda()
+    want = _reference_run(pf, x, 6)
+    out = torch.zeros_like(x)
+    assert _run_noalloc(pf, x, out, 6, None) == 0
+    torch.cuda.synchronize()
+    assert rel_err(pf.unpack(out.cpu().numpy()), pf.unpack(want.cpu().numpy()))[0] <= 1e-12
+    assert _run_noalloc(pf, x, out, 4, None) == 1
