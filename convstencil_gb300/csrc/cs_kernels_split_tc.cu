@@ -137,52 +137,72 @@ constexpr unsigned long long kF64Bias = 256ull * ((1ull << 54) - 1) / 511;
 
 // Biased-digit word of one FP64 value (bits lo, hi) of a tile whose largest
 // biased exponent is eb1 (at least 1): X = round(x / 2^(eb1 - 1074)), so
-// |X| <= 2^52, returned as X + kF64Bias.
+// |X| <= 2^52, returned as X + kF64Bias. The shift is clamped at 63: any
+// mantissa (< 2^53) shifted by 55 or more rounds to 0 as it should.
 __device__ __forceinline__ unsigned long long f64_biased_fixed(unsigned lo, unsigned hi, int eb1)
 {
     const int e = (int)((hi >> 20) & 0x7FFu);
     const int ee = max(e, 1);  // subnormals: no implicit bit, exponent 1
     const unsigned long long mant =
         ((unsigned long long)((hi & 0xFFFFFu) | (e ? 0x100000u : 0u)) << 32) | lo;
-    const int s = eb1 + 1 - ee;  // >= 1
-    const unsigned long long x = s < 56 ? ((mant >> (s - 1)) + 1) >> 1 : 0ull;  // round half up
-    return (hi >> 31) ? kF64Bias - x : kF64Bias + x;
+    const unsigned long long x = ((mant >> min(eb1 - ee, 63)) + 1) >> 1;  // round half up
+    const unsigned long long neg = (unsigned long long)(long long)((int)hi >> 31);  // 0 or all ones
+    return (kF64Bias - neg) + (x ^ neg);  // kF64Bias + x, or kF64Bias - x = (kF64Bias + 1) + ~x
 }
 
 // Digit k (0 = most significant) of two biased words, as an FP16 pair:
 // FP16 (1024 + u) has the bits 0x6400 | u, and (1024 + u) - 1280 = u - 256
-// is exact in FP16.
+// is exact in FP16. (The top field is at most 384, so masking it is harmless.)
 template <int K>
 __device__ __forceinline__ unsigned f64_digit_pair(unsigned long long ya, unsigned long long yb)
 {
     constexpr int sh = kDigitBits * (5 - K);
-    unsigned ua = (unsigned)(ya >> sh), ub = (unsigned)(yb >> sh);
-    if constexpr (K > 0) {
-        ua &= 511u;
-        ub &= 511u;
-    }
-    const unsigned w = (ua | (ub << 16)) | 0x64006400u;
+    const unsigned ta = (unsigned)(ya >> sh);
+    const unsigned tb = sh >= 16 ? (unsigned)(yb >> (sh - 16)) : (unsigned)(yb << (16 - sh));
+    const unsigned w = ((ta & 0x1FFu) | (tb & 0x1FF0000u)) | 0x64006400u;
     const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&w), __halves2half2(__ushort_as_half(0x6500),
                                                                                      __ushort_as_half(0x6500)));
     return *reinterpret_cast<const unsigned *>(&h);
 }
 
-// FP64 value of T * 2^(be0 - 1086), rounded to nearest even, from integer
-// operations; results outside the normal range take the FP64 route.
-__device__ __forceinline__ double f64_from_fixed(long long t, int be0)
+// T = sum over levels of S_L 2^(42 - 9L), level 5 without its last three
+// bits: |T| < 2^63. Multiply-adds on the FMA pipe (the integer ALU pipe is
+// this kernel's busiest).
+__device__ __forceinline__ long long f64_combine(const float (&lv)[6])
 {
-    if (t == 0) return 0.0;
-    const unsigned long long sign = (unsigned long long)t & 0x8000000000000000ull;
-    const unsigned long long a = t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
-    const int lz = __clzll((long long)a);
-    const unsigned long long an = a << lz;  // bit 63 set
-    const unsigned long long mant = an >> 11;
-    const unsigned rb = (unsigned)an & 0x7FFu;
-    const unsigned long long up = (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
-    const int be = be0 - lz;  // biased exponent of the result
-    if (be >= 1 && be <= 2046)
-        return __longlong_as_double((long long)(sign | ((((unsigned long long)(be - 1)) << 52) + mant + up)));
-    return scalbn((double)t, be0 - 1086);  // subnormal or overflowing results
+    long long t = (long long)(__float2int_rn(lv[5]) >> 3);
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(t) : "r"(__float2int_rn(lv[4])), "r"(1 << 6));
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(t) : "r"(__float2int_rn(lv[3])), "r"(1 << 15));
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(t) : "r"(__float2int_rn(lv[2])), "r"(1 << 24));
+    unsigned tl, th;
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(tl), "=r"(th) : "l"(t));
+    // levels 0 and 1 sit wholly in the upper word: S1 2^33 + S0 2^42
+    th += (unsigned)(__float2int_rn(lv[1]) * 2 + __float2int_rn(lv[0]) * 1024);
+    asm("mov.b64 %0, {%1, %2};" : "=l"(t) : "r"(tl), "r"(th));
+    return t;
+}
+
+// Results outside the normal FP64 range (subnormal or overflowing): FP64
+// arithmetic, kept out of line so that the common path carries no FP64
+// instruction (the compiler cannot if-convert a call).
+__device__ __noinline__ double f64_from_fixed_rare(long long t, int c)
+{
+    return scalbn((double)t, c);
+}
+
+// FP64 value of T * 2^c, rounded to nearest even: the 64-bit integer is
+// converted once (cvt.rn.f64.s64, exact rounding) and the power of two is
+// added to the exponent field; results outside the normal range take the
+// out-of-line FP64 route.
+__device__ __forceinline__ double f64_from_fixed(long long t, int c)
+{
+    const double d = __ll2double_rn(t);
+    const long long bits = __double_as_longlong(d);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    const int ne = e + c;
+    if (e == 0) return d;  // t == 0
+    if (ne >= 1 && ne <= 2046) return __longlong_as_double(bits + ((long long)c << 52));
+    return f64_from_fixed_rare(t, c);
 }
 
 // Marks a tile whose window holds an Inf or NaN (its outputs become NaN).
@@ -481,20 +501,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int yy = y0 + R * er + rho;
                 if (yy >= m) continue;
                 if constexpr (F::kF64) {
-                    // T = sum over levels of S_L 2^(42 - 9L) (level 5 without
-                    // its last three bits): |T| < 2^63; value T 2^(be0 - 1086).
-                    const int be0 = ex + sw.ew + 6;
+                    // value = T 2^c with T from the levels (f64_combine) and
+                    // c = (input scale) + (weight scale) - 1080.
+                    const int c = ex + sw.ew - 1080;
                     double res[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const long long t = ((long long)__float2int_rn(acc[0][j]) << 42) +
-                                            ((long long)__float2int_rn(acc[1][j]) << 33) +
-                                            ((long long)__float2int_rn(acc[2][j]) << 24) +
-                                            ((long long)__float2int_rn(acc[3][j]) << 15) +
-                                            ((long long)__float2int_rn(acc[4][j]) << 6) +
-                                            (long long)(__float2int_rn(acc[5][j]) >> 3);
+                        const float lv[6] = {acc[0][j], acc[1][j], acc[2][j], acc[3][j], acc[4][j], acc[5][j]};
                         res[j] = ex == kNonFiniteTile ? __longlong_as_double(0x7FF8000000000000ll)
-                                                      : f64_from_fixed(t, be0);
+                                                      : f64_from_fixed(f64_combine(lv), c);
                     }
                     double *o = reinterpret_cast<double *>(out) + (long long)yy * ld + xb;
 #pragma unroll
