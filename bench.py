@@ -568,6 +568,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-oracle", action="store_true", help="skip the whole-grid oracle comparison")
+    ap.add_argument("--split-algo", default="auto", choices=["auto", "tc", "mma", "mma_tma", "fma"],
+                    help="pin the split kernel (default: the plan's tuner); for profiler runs, whose "
+                         "serialised launches distort the tuner's timings")
+    ap.add_argument("--fp64-algo", default="auto", choices=["auto", "tc", "fma", "mma"],
+                    help="pin the FP64 kernel (default: the plan's tuner)")
     ap.add_argument("--served", type=int, default=96,
                     help="requests in the served-stream sample (0 = skip)")
     ap.add_argument("--served-rate", type=float, default=40.0, help="Poisson arrival rate (req/s)")
@@ -658,7 +663,7 @@ def main():
     results = {}
     results = {}
     pts = float(M) * N
-    peaks_now = pipe_peaks()  # measured now, on this GPU
+    peaks_now = {}  # FP64 pipe rate, measured when an FP64-pipe kernel needs it (fp64_roof)
 
     if args.served_only:
         line = {"served": served_stream(args.served, args.served_rate, 17 + rank, local) if args.served else None}
@@ -670,6 +675,9 @@ def main():
 
     # ---------------- FP64 path (the drop-in form; the plan's tuner picks the kernel)
     p64 = cs.Plan(SHAPE, (M, N), w)
+    if args.fp64_algo != "auto":
+        p64.set_option(cs.Option.ALGO, {"tc": cs.Algo.FP64_TC, "fma": cs.Algo.FP64_FMA,
+                                        "mma": cs.Algo.FP64_MMA}[args.fp64_algo])
     host = p64.pack(x)
     a64 = torch.from_numpy(host).to(dev)
     b64 = torch.zeros_like(a64)
@@ -689,6 +697,10 @@ def main():
     split_ok = True
     try:
         psp = cs.Plan(SHAPE, (M, N), w, precision=cs.Precision.SPLIT)
+        if args.split_algo != "auto":
+            psp.set_option(cs.Option.ALGO, {"tc": cs.Algo.SPLIT_TC, "mma": cs.Algo.SPLIT_MMA,
+                                            "mma_tma": cs.Algo.SPLIT_MMA_TMA,
+                                            "fma": cs.Algo.SPLIT_FMA}[args.split_algo])
     except cs.ConvStencilError:
         split_ok = False
     if split_ok:
@@ -892,6 +904,8 @@ def fp64_roof(r, pts, peaks_now, hbm_roof):
     (no FP64 instruction), the FP64 pipe (measured now) for the FMA/MMA ones."""
     if r["algo"] == "FP64_TC":
         return hbm_roof(r["kernel_s"], "k2d_tc<FmtF64> (FP64_TC)", "fp64_tc_box2d3r_sweep")
+    if not peaks_now:
+        peaks_now.update(pipe_peaks())  # measured now, on this GPU
     pk = peaks_now.get("fp64 fma")
     ach = 2.0 * TAPS * pts / r["kernel_s"] / 1e12
     return {"bound": "fp64 pipe", "achieved": round(ach, 4), "peak": pk, "unit": "TFLOP/s",

@@ -87,6 +87,7 @@ class Option(enum.IntEnum):
     TIME_BLOCK = 3
     WAIT_LIMIT_US = 4
     WAIT_TEST_SKIP_LOADS = 5
+    TILE_ROWS = 6
 
 
 class Layout(ctypes.Structure):
@@ -155,6 +156,7 @@ def lib() -> ctypes.CDLL:
     L.cs_plan_destroy.argtypes = [vp]
     L.cs_plan_get_algo.argtypes = [vp, ctypes.POINTER(i)]
     L.cs_plan_get_time_block.argtypes = [vp, ctypes.POINTER(i)]
+    L.cs_plan_get_tile_rows.argtypes = [vp, ctypes.POINTER(i)]
     L.cs_run.argtypes = [vp, vp, vp, ll, vp, ctypes.POINTER(i)]
     L.cs_run_host.argtypes = [vp, dp, dp, ll]
     L.cs_split_from_fp64.argtypes = [vp, vp, vp, vp]
@@ -286,6 +288,13 @@ class Plan:
         """Steps per launch of the last run (temporal blocking; 1 = off)."""
         t = ctypes.c_int()
         check(lib().cs_plan_get_time_block(self._h, ctypes.byref(t)))
+        return int(t.value)
+
+    @property
+    def tile_rows(self) -> int:
+        """Rows per CTA tile of the FP64 FMA 2D kernel in the last run (0: another kernel)."""
+        t = ctypes.c_int()
+        check(lib().cs_plan_get_tile_rows(self._h, ctypes.byref(t)))
         return int(t.value)
 
     def sweeps(self, steps: int) -> int:

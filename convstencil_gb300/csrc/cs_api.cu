@@ -210,6 +210,7 @@ void native_layout(int dims, int r, const long long *ext, cs_layout &L)
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int, int>, int> g_tune;      // -> algorithm
 std::map<std::tuple<int, int, int, int, int>, int> g_tune_tb;   // -> steps per launch (split FMA)
+std::map<std::tuple<int, int, int, int, int>, int> g_tune_rows; // -> FP64 FMA 2D tile rows
 
 }  // namespace
 
@@ -225,6 +226,8 @@ struct cs_plan {
     int last_algo = CS_ALGO_AUTO;  // kernel family the last cs_run used
     int time_block = 0;            // split FMA: steps per launch (0 = tuner)
     int last_time_block = 1;
+    int tile_rows = 0;             // FP64 FMA 2D: rows per CTA tile (0 = tuner)
+    int active_rows = 0;           // the tile rows launches use now (0 = by grid size)
     long long reanchor = 100;
     cs::TcWait wait;               // bounded waits of the tcgen05 kernels
     // Small grids: blocks of sweeps replayed as CUDA graphs (see cs_run).
@@ -259,11 +262,13 @@ bool split_mma_ok(const cs_plan *p)
 // FP64 plans of 2D radius-3 stencils (any 7x7 weights) also run on the
 // tcgen05 digit pipeline; like the split slice kernels its error is relative
 // to the tile's scale, so grids smaller than the 8x8 window stay on FP64 FMA.
-bool fp64_tc_ok(const cs_plan *p)
+bool fp64_tc_geometry_ok(const cs_plan *p)
 {
-    return p->prec == CS_PREC_FP64 && p->dims == 2 && p->radius == 3 && p->view.ext[0] >= 8 &&
-           p->view.ext[1] >= 8 && cs::split_mma_layout_ok(p->view, p->layout.origin);
+    return p->dims == 2 && p->radius == 3 && p->view.ext[0] >= 8 && p->view.ext[1] >= 8 &&
+           cs::split_mma_layout_ok(p->view, p->layout.origin);
 }
+
+bool fp64_tc_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc_geometry_ok(p); }
 
 // Split plans of 3D radius-1 stencils (27 weights) also run on the tcgen05
 // slice kernel.
@@ -284,7 +289,7 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
             cs::split_tma_layout_ok(p->view, off, in_base))
             return cs::launch_fp64_sweep_tc(p->view, p->w, off, p->layout.elements, (const double *)in_base,
                                             (double *)out_base, p->wait, st);
-        return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st);
+        return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st, p->active_rows);
     }
     // The tensor-core split kernels store float4 (two points) at even element
     // offsets, so they need a 16-byte aligned output base; the TMA-fed ones
@@ -462,7 +467,214 @@ cs_status choose_time_block(cs_plan *p, int algo, const void *a, void *b, cudaSt
     return CS_OK;
 }
 
+// Tile rows of the FP64 FMA 2D kernel (16 or 32 rows per CTA tile): with
+// tile_rows 0 the first run times both once on a -> b (bitwise the same
+// sweep) and remembers the faster for plans of the same class.
+cs_status choose_tile_rows(cs_plan *p, int algo, const void *a, void *b, cudaStream_t st, int *out)
+{
+    *out = 0;
+    if (p->prec != CS_PREC_FP64 || algo != CS_ALGO_FP64_FMA || p->dims != 2) return CS_OK;
+    if (p->tile_rows > 0) {
+        *out = p->tile_rows;
+        return CS_OK;
+    }
+    auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_rows.find(key);
+        if (it != g_tune_rows.end()) {
+            *out = it->second;
+            return CS_OK;
+        }
+    }
+    const long long off = p->layout.origin;
+    cudaEvent_t e0, e1;
+    CS_CUDA(cudaEventCreate(&e0));
+    CS_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_rows = 32;
+    for (int rep = 0; rep < 2; ++rep) {
+        for (int rows : {16, 32}) {
+            CS_CUDA(cudaEventRecord(e0, st));
+            cudaError_t e = cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, (const double *)a + off,
+                                                (double *)b + off, st, rows);
+            if (e != cudaSuccess) return cuda_fail(e, "tile-rows tuning launch");
+            CS_CUDA(cudaEventRecord(e1, st));
+            CS_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep == 1 && ms < best) {
+                best = ms;
+                best_rows = rows;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_rows[key] = best_rows;
+    }
+    *out = best_rows;
+    return CS_OK;
+}
+
 }  // namespace
+
+namespace cs {
+
+// FP64 re-anchor sweep of a split plan: the (hi, lo) state in `src` is
+// turned into FP64 in place, one sweep runs in FP64 arithmetic (the tcgen05
+// digit pipeline for 2D radius-3 plans where the buffers allow it, else FP64
+// FMA) into `dst`, and `dst` is turned back into (hi, lo) pairs in place. The
+// halos read the same either way (0.0 has the bits of (0, 0)); `src` is left
+// holding FP64 values, like any consumed ping-pong buffer.
+// One FP64 sweep of the plan's stencil between FP64 buffers.
+cudaError_t fp64_anchor_sweep_fp64_in(const cs_plan *p, const void *src, void *dst, cudaStream_t st)
+{
+    const long long n = p->layout.elements, off = p->layout.origin;
+    if (fp64_tc_geometry_ok(p) && reinterpret_cast<uintptr_t>(dst) % 16 == 0 && split_tma_layout_ok(p->view, off, src))
+        return launch_fp64_sweep_tc(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
+    return launch_fp64_fma(p->view, p->radius, p->pattern, p->w, (const double *)src + off, (double *)dst + off, st);
+}
+
+cudaError_t fp64_anchor_sweep(const cs_plan *p, void *src, void *dst, cudaStream_t st)
+{
+    const long long n = p->layout.elements;
+    cudaError_t e = launch_split_to_fp64_inplace(n, src, st);
+    if (e == cudaSuccess) e = fp64_anchor_sweep_fp64_in(p, src, dst, st);
+    if (e == cudaSuccess) e = launch_fp64_to_split_inplace(n, dst, st);
+    return e;
+}
+
+// cs_run with the sweeps numbered from first_sweep: split plans run sweep k
+// in FP64 when (k + 1) is a multiple of the re-anchor interval, so a run cut
+// into chunks (the server) re-anchors where one whole run would.
+cs_status run_from(cs_plan *p, void *a, void *b, long long first_sweep, long long steps, cudaStream_t st,
+                   int *result_in_b)
+{
+    if (!p || !a || !b) return fail(CS_ERR_INVALID_ARGUMENT, "NULL plan or buffer");
+    if (a == b) return fail(CS_ERR_INVALID_ARGUMENT, "ping-pong buffers must differ");
+    if (reinterpret_cast<uintptr_t>(a) % 8 || reinterpret_cast<uintptr_t>(b) % 8)
+        return fail(CS_ERR_INVALID_ARGUMENT, "grid buffers must be 8-byte aligned (double / float2 elements)");
+    long long sweeps = 0;
+    cs_status s = cs_plan_sweeps(p, steps, &sweeps);
+    if (s != CS_OK) return s;
+    int algo = CS_ALGO_FP64_FMA, tb = 1;
+    if (sweeps > 0) {
+        s = choose_algo(p, a, b, st, &algo);
+        if (s != CS_OK) return s;
+        s = choose_time_block(p, algo, a, b, st, &tb);
+        if (s != CS_OK) return s;
+        int rows = 0;
+        s = choose_tile_rows(p, algo, a, b, st, &rows);
+        if (s != CS_OK) return s;
+        p->last_algo = algo;
+        p->last_time_block = tb;
+        p->active_rows = rows;
+    }
+    void *buf[2] = {a, b};
+    int cur = 0;
+    const long long off = p->layout.origin;
+    // One launch of t sweeps from buf[c] to buf[c ^ 1] on stream `on`.
+    auto one_launch = [&](int t, int c, cudaStream_t on) -> cudaError_t {
+        if (t >= 2)
+            return cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w,
+                                             (const float2 *)buf[c] + off, (float2 *)buf[c ^ 1] + off, on);
+        return launch_sweep(p, algo, buf[c], buf[c ^ 1], on);
+    };
+    // Sweep i of this call is an FP64 re-anchor sweep.
+    auto anchor = [&](long long i) {
+        return p->prec == CS_PREC_SPLIT && p->reanchor > 0 && (first_sweep + i + 1) % p->reanchor == 0;
+    };
+    // Small grids spend a noticeable share of each sweep on launch gaps, so
+    // blocks of an even number of launches are captured once as a CUDA graph
+    // and replayed: same kernels, same order, same re-anchoring points, so the
+    // result is bitwise the one of plain launches. Not used while the caller
+    // is itself capturing `stream` (its capture records plain launches).
+    long long pts = 1;
+    for (int d = 0; d < p->dims; ++d) pts *= p->view.ext[d];
+    const int glaunches = std::max(2, (cs::kGraphBlockSweeps / tb) & ~1);
+    const long long gsweeps = (long long)glaunches * tb;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const bool graphs = pts <= cs::kGraphMaxPoints && sweeps >= 3 * gsweeps &&
+                        cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone;
+    // The graph of a block starting at buf[c], captured on the plan's private
+    // stream the first time and cached in the plan.
+    auto block_graph = [&](int c, cudaGraphExec_t *out) -> cs_status {
+        std::lock_guard<std::mutex> lk(p->graph_mu);
+        const auto key = std::make_tuple((const void *)buf[c], (const void *)buf[c ^ 1], algo, tb * 64 + p->active_rows,
+                                         glaunches);
+        auto it = p->graphs.find(key);
+        if (it != p->graphs.end()) {
+            *out = it->second;
+            return CS_OK;
+        }
+        if (!p->capture_stream)
+            CS_CUDA(cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking));
+        CS_CUDA(cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = cs::g_launches.load();
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < glaunches && e == cudaSuccess; ++k)
+            e = one_launch(tb, c ^ (k & 1), p->capture_stream);
+        cs::note_launch(before - cs::g_launches.load());  // captured, not run: counted at each replay
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(e != cudaSuccess ? e : e2, "sweep capture");
+        }
+        cudaGraphExec_t ge = nullptr;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+        p->graphs[key] = ge;
+        *out = ge;
+        return CS_OK;
+    };
+    for (long long i = 0; i < sweeps;) {
+        if (anchor(i)) {  // this sweep in FP64 (same buffer parity as any sweep)
+            cudaError_t e = fp64_anchor_sweep(p, buf[cur], buf[cur ^ 1], st);
+            if (e != cudaSuccess) return cuda_fail(e, "re-anchor sweep");
+            cur ^= 1;
+            ++i;
+            continue;
+        }
+        // The first launch of a run is always plain, so any first-launch
+        // set-up of a kernel has happened before a capture.
+        if (graphs && i > 0 && sweeps - i >= gsweeps) {
+            bool clean = true;  // no re-anchor sweep inside the block
+            for (long long k = i; k < i + gsweeps; ++k)
+                if (anchor(k)) clean = false;
+            if (clean) {
+                cudaGraphExec_t ge = nullptr;
+                cs_status gs = block_graph(cur, &ge);
+                if (gs != CS_OK) return gs;
+                cudaError_t e = cudaGraphLaunch(ge, st);
+                if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+                cs::note_launch(glaunches);
+                i += gsweeps;  // even launch count: back in buf[cur]
+                continue;
+            }
+        }
+        // A temporally blocked launch stops short of the next re-anchor sweep.
+        int t = (int)std::min<long long>(tb, sweeps - i);
+        for (int k = 1; k < t; ++k)
+            if (anchor(i + k)) {
+                t = k;
+                break;
+            }
+        cudaError_t e = one_launch(t, cur, st);
+        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        cur ^= 1;
+        i += t;
+    }
+    if (result_in_b) *result_in_b = cur;
+    return CS_OK;
+}
+
+
+}  // namespace cs
 
 extern "C" {
 
@@ -602,6 +814,12 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
                         "temporal blocking serves split-precision 2D radius-1 and 1D plans");
         p->time_block = (int)v;
         return CS_OK;
+    case CS_OPT_TILE_ROWS:
+        if (v != 0 && v != 16 && v != 32) return fail(CS_ERR_INVALID_ARGUMENT, "tile rows must be 0 (tuner), 16 or 32");
+        if (v != 0 && !(p->prec == CS_PREC_FP64 && p->dims == 2))
+            return fail(CS_ERR_UNSUPPORTED, "tile rows apply to FP64 2D plans (FMA kernel)");
+        p->tile_rows = (int)v;
+        return CS_OK;
     case CS_OPT_WAIT_LIMIT_US:
         if (v < 1 || v > 60000000LL)
             return fail(CS_ERR_INVALID_ARGUMENT, "wait limit must be 1 .. 60,000,000 microseconds");
@@ -640,6 +858,13 @@ CS_API cs_status cs_plan_get_algo(const cs_plan *p, int *algo)
     return CS_OK;
 }
 
+CS_API cs_status cs_plan_get_tile_rows(const cs_plan *p, int *rows)
+{
+    if (!p || !rows) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
+    *rows = p->active_rows;
+    return CS_OK;
+}
+
 CS_API cs_status cs_plan_get_time_block(const cs_plan *p, int *steps_per_launch)
 {
     if (!p || !steps_per_launch) return fail(CS_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -655,116 +880,7 @@ CS_API cs_status cs_plan_destroy(cs_plan *p)
 
 CS_API cs_status cs_run(cs_plan *p, void *a, void *b, long long steps, void *stream, int *result_in_b)
 {
-    if (!p || !a || !b) return fail(CS_ERR_INVALID_ARGUMENT, "NULL plan or buffer");
-    if (a == b) return fail(CS_ERR_INVALID_ARGUMENT, "ping-pong buffers must differ");
-    if (reinterpret_cast<uintptr_t>(a) % 8 || reinterpret_cast<uintptr_t>(b) % 8)
-        return fail(CS_ERR_INVALID_ARGUMENT, "grid buffers must be 8-byte aligned (double / float2 elements)");
-    long long sweeps = 0;
-    cs_status s = cs_plan_sweeps(p, steps, &sweeps);
-    if (s != CS_OK) return s;
-    cudaStream_t st = (cudaStream_t)stream;
-    int algo = CS_ALGO_FP64_FMA, tb = 1;
-    if (sweeps > 0) {
-        s = choose_algo(p, a, b, st, &algo);
-        if (s != CS_OK) return s;
-        s = choose_time_block(p, algo, a, b, st, &tb);
-        if (s != CS_OK) return s;
-        p->last_algo = algo;
-        p->last_time_block = tb;
-    }
-    void *buf[2] = {a, b};
-    int cur = 0;
-    const long long off = p->layout.origin;
-    // One launch of t sweeps from buf[c] to buf[c ^ 1] on stream `on`.
-    auto one_launch = [&](int t, int c, cudaStream_t on) -> cudaError_t {
-        if (t >= 2)
-            return cs::launch_split_sweep_tb(p->view, p->radius, p->pattern, t, p->w,
-                                             (const float2 *)buf[c] + off, (float2 *)buf[c ^ 1] + off, on);
-        return launch_sweep(p, algo, buf[c], buf[c ^ 1], on);
-    };
-    auto reanchor_after = [&](long long start, long long done) {
-        return p->prec == CS_PREC_SPLIT && p->reanchor > 0 && done / p->reanchor != start / p->reanchor;
-    };
-    // Small grids spend a noticeable share of each sweep on launch gaps, so
-    // blocks of an even number of launches are captured once as a CUDA graph
-    // and replayed: same kernels, same order, same re-anchoring points, so the
-    // result is bitwise the one of plain launches. Not used while the caller
-    // is itself capturing `stream` (its capture records plain launches).
-    long long pts = 1;
-    for (int d = 0; d < p->dims; ++d) pts *= p->view.ext[d];
-    const int glaunches = std::max(2, (cs::kGraphBlockSweeps / tb) & ~1);
-    const long long gsweeps = (long long)glaunches * tb;
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    const bool graphs = pts <= cs::kGraphMaxPoints && sweeps >= 3 * gsweeps &&
-                        cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone;
-    // The graph of a block starting at buf[c], captured on the plan's private
-    // stream the first time and cached in the plan.
-    auto block_graph = [&](int c, cudaGraphExec_t *out) -> cs_status {
-        std::lock_guard<std::mutex> lk(p->graph_mu);
-        const auto key = std::make_tuple((const void *)buf[c], (const void *)buf[c ^ 1], algo, tb, glaunches);
-        auto it = p->graphs.find(key);
-        if (it != p->graphs.end()) {
-            *out = it->second;
-            return CS_OK;
-        }
-        if (!p->capture_stream)
-            CS_CUDA(cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking));
-        CS_CUDA(cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal));
-        const long long before = cs::g_launches.load();
-        cudaError_t e = cudaSuccess;
-        for (int k = 0; k < glaunches && e == cudaSuccess; ++k)
-            e = one_launch(tb, c ^ (k & 1), p->capture_stream);
-        cs::note_launch(before - cs::g_launches.load());  // captured, not run: counted at each replay
-        cudaGraph_t g = nullptr;
-        const cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &g);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return cuda_fail(e != cudaSuccess ? e : e2, "sweep capture");
-        }
-        cudaGraphExec_t ge = nullptr;
-        e = cudaGraphInstantiate(&ge, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
-        p->graphs[key] = ge;
-        *out = ge;
-        return CS_OK;
-    };
-    for (long long i = 0; i < sweeps;) {
-        // The first launch of a run is always plain, so any first-launch
-        // set-up of a kernel has happened before a capture.
-        if (graphs && i > 0 && sweeps - i >= gsweeps) {
-            bool clean = true;  // no re-anchor inside the block (one after its last launch is fine)
-            for (int k = 0; k + 1 < glaunches; ++k)
-                if (reanchor_after(i + (long long)k * tb, i + (long long)(k + 1) * tb)) clean = false;
-            if (clean) {
-                cudaGraphExec_t ge = nullptr;
-                cs_status gs = block_graph(cur, &ge);
-                if (gs != CS_OK) return gs;
-                cudaError_t e = cudaGraphLaunch(ge, st);
-                if (e != cudaSuccess) return cuda_fail(e, "graph launch");
-                cs::note_launch(glaunches);
-                const long long done = i + gsweeps;  // even launch count: back in buf[cur]
-                if (reanchor_after(done - tb, done)) {
-                    e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[cur], st);
-                    if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
-                }
-                i = done;
-                continue;
-            }
-        }
-        const int t = (int)std::min<long long>(tb, sweeps - i);
-        cudaError_t e = one_launch(t, cur, st);
-        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
-        cur ^= 1;
-        const long long done = i + t;
-        if (reanchor_after(i, done)) {
-            e = cs::launch_split_reanchor(p->layout.elements, (float2 *)buf[cur], st);
-            if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
-        }
-        i = done;
-    }
-    if (result_in_b) *result_in_b = cur;
-    return CS_OK;
+    return cs::run_from(p, a, b, 0, steps, (cudaStream_t)stream, result_in_b);
 }
 
 CS_API cs_status cs_split_from_fp64(const cs_plan *p, const double *src, void *dst, void *stream)
@@ -1075,12 +1191,25 @@ cs_status run_into(cs_plan *p, const void *in, void *out, void *scratch, long lo
     const void *src = in;
     for (long long i = 1; i <= sweeps; ++i) {
         void *dst = ((sweeps - i) % 2 == 0) ? out : scratch;
-        cudaError_t e = launch_sweep(p, algo, src, dst, st);
-        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+        cudaError_t e;
         if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && (i % p->reanchor) == 0) {
-            e = launch_split_reanchor(p->layout.elements, (float2 *)dst, st);
-            if (e != cudaSuccess) return cuda_fail(e, "re-anchor launch");
+            if (src == in) {
+                // `in` stays untouched: its FP64 form goes to dst, the FP64
+                // sweep into the third buffer, and back to (hi, lo) in dst.
+                void *third = dst == out ? scratch : out;
+                e = launch_split_to_fp64(p->layout.elements, (const float2 *)in, (double *)dst, st);
+                if (e == cudaSuccess) {
+                    e = fp64_anchor_sweep_fp64_in(p, dst, third, st);
+                    if (e == cudaSuccess)
+                        e = launch_split_from_fp64(p->layout.elements, (const double *)third, (float2 *)dst, st);
+                }
+            } else {
+                e = fp64_anchor_sweep(p, const_cast<void *>(src), dst, st);
+            }
+        } else {
+            e = launch_sweep(p, algo, src, dst, st);
         }
+        if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
         src = dst;
     }
     return CS_OK;
@@ -1092,7 +1221,7 @@ struct PlanFacts {
     int dims, radius, pattern, steps_per_sweep;
     cs_precision prec;
     GridView view;
-    long long origin;
+    long long origin, elements;
     const Weights *w;
 };
 
@@ -1106,6 +1235,7 @@ bool plan_facts(const cs_plan *p, PlanFacts *f)
     f->prec = p->prec;
     f->view = p->view;
     f->origin = p->layout.origin;
+    f->elements = p->layout.elements;
     f->w = &p->w;
     return true;
 }

@@ -35,8 +35,9 @@ struct GridView {
 // Kernel entry points (cs_kernels_fp64.cu). Each launches one sweep
 // in -> out on `stream`; `in`/`out` address interior point 0. Returns
 // cudaSuccess or the launch error.
+// tile_rows (2D only): 16 or 32 rows per CTA tile, 0 = by grid size.
 cudaError_t launch_fp64_fma(const GridView &g, int radius, int pattern, const Weights &w,
-                            const double *in, double *out, cudaStream_t stream);
+                            const double *in, double *out, cudaStream_t stream, int tile_rows = 0);
 // FP64 tensor-core path (mma.sync m8n8k4.f64), 2D radius-3 dense kernels only.
 cudaError_t launch_fp64_mma_2d(const GridView &g, const Weights &w, const double *in, double *out,
                                cudaStream_t stream);
@@ -80,6 +81,17 @@ cudaError_t launch_split_sweep_tc(const GridView &g, const Weights &w, long long
 cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long origin, long long elements,
                                  const double *in_base, double *out_base, const TcWait &wait,
                                  cudaStream_t stream);
+// Batches of 2D radius-3 grids on the tcgen05 kernels (split or FP64): one
+// device record per grid (tc_batch_record_bytes each, 128-byte aligned)
+// holding its tensor map over `in_base`, output, sizes, first tile and
+// weight digits; tiles of a grid are numbered from tile_begin and *tiles
+// returns their count. One launch advances every grid by one sweep.
+size_t tc_batch_record_bytes(bool fp64);
+cudaError_t tc_batch_fill_record(bool fp64, void *rec, const GridView &g, const Weights &w, long long origin,
+                                 long long elements, const void *in_base, void *out_base, int tile_begin,
+                                 int *tiles);
+cudaError_t launch_tc_batch(bool fp64, const void *records, int ngrids, int total_tiles, const TcWait &wait,
+                            cudaStream_t stream);
 // 2D tensor map over a whole (hi, lo) buffer of `rows` x `ld` pairs, box_x x box_y tiles.
 cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long long ld, long long rows,
                                     unsigned box_x, unsigned box_y);
@@ -101,10 +113,13 @@ int device_sm_count();
 cudaError_t split_wait_timeouts(unsigned *count, bool reset);
 cudaError_t split_tc_wait_timeouts(unsigned *count, bool reset);
 cudaError_t split_tc3d_wait_timeouts(unsigned *count, bool reset);
-// Whole-buffer conversions and re-anchoring over n elements.
+// Whole-buffer conversions over n elements, and the in-place forms used by
+// the FP64 re-anchor sweeps ((hi, lo) pairs and FP64 values share a buffer
+// layout: 8 bytes per point).
 cudaError_t launch_split_from_fp64(long long n, const double *src, float2 *dst, cudaStream_t stream);
 cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cudaStream_t stream);
-cudaError_t launch_split_reanchor(long long n, float2 *grid, cudaStream_t stream);
+cudaError_t launch_split_to_fp64_inplace(long long n, void *grid, cudaStream_t stream);
+cudaError_t launch_fp64_to_split_inplace(long long n, void *grid, cudaStream_t stream);
 
 // Process-wide launch counter (host side), for the bench's launch accounting.
 void note_launch(long long n = 1);

@@ -264,13 +264,17 @@ int z_chunk(const GridView &g)
 }
 
 
+// Rows per CTA tile: 16 (4 per thread) or 32 (8 per thread); 0 picks 16 on
+// grids too small to give every SM several 32-row tiles. Both tile shapes sum
+// every point's taps in the same order, so results do not depend on it.
 template <int R, int P>
-cudaError_t go2d(const GridView &g, const Weights &w, const double *in, double *out,
+cudaError_t go2d(const GridView &g, const Weights &w, const double *in, double *out, int tile_rows,
                  cudaStream_t st)
 {
     constexpr int K = 2 * R + 1;
     const unsigned gx = ceil_div(g.ext[1], 64);
-    if ((long long)gx * ceil_div(g.ext[0], 32) < 6LL * device_sm_count()) {
+    if (tile_rows == 0) tile_rows = (long long)gx * ceil_div(g.ext[0], 32) < 6LL * device_sm_count() ? 16 : 32;
+    if (tile_rows == 16) {
         dim3 grid(gx, ceil_div(g.ext[0], 16));
         k2d_fma<R, P, 4><<<grid, 256, 0, st>>>(in, out, (int)g.ext[0], (int)g.ext[1], g.pitch[0],
                                                 pack<K * K>(w));
@@ -317,7 +321,7 @@ bool fp64_fma_supported(int dims, int radius, int pattern)
 }
 
 cudaError_t launch_fp64_fma(const GridView &g, int R, int P, const Weights &w, const double *in,
-                            double *out, cudaStream_t st)
+                            double *out, cudaStream_t st, int tile_rows)
 {
     note_launch();
     if (g.dims == 1) {
@@ -329,18 +333,18 @@ cudaError_t launch_fp64_fma(const GridView &g, int R, int P, const Weights &w, c
         }
     } else if (g.dims == 2) {
         if (R == 1) {
-            if (P == PAT_STAR) return go2d<1, PAT_STAR>(g, w, in, out, st);
-            return go2d<1, PAT_DENSE>(g, w, in, out, st);
+            if (P == PAT_STAR) return go2d<1, PAT_STAR>(g, w, in, out, tile_rows, st);
+            return go2d<1, PAT_DENSE>(g, w, in, out, tile_rows, st);
         }
         if (R == 2) {
-            if (P == PAT_STAR) return go2d<2, PAT_STAR>(g, w, in, out, st);
-            if (P == PAT_DIAMOND) return go2d<2, PAT_DIAMOND>(g, w, in, out, st);
-            return go2d<2, PAT_DENSE>(g, w, in, out, st);
+            if (P == PAT_STAR) return go2d<2, PAT_STAR>(g, w, in, out, tile_rows, st);
+            if (P == PAT_DIAMOND) return go2d<2, PAT_DIAMOND>(g, w, in, out, tile_rows, st);
+            return go2d<2, PAT_DENSE>(g, w, in, out, tile_rows, st);
         }
         if (R == 3) {
-            if (P == PAT_STAR) return go2d<3, PAT_STAR>(g, w, in, out, st);
-            if (P == PAT_DIAMOND) return go2d<3, PAT_DIAMOND>(g, w, in, out, st);
-            return go2d<3, PAT_DENSE>(g, w, in, out, st);
+            if (P == PAT_STAR) return go2d<3, PAT_STAR>(g, w, in, out, tile_rows, st);
+            if (P == PAT_DIAMOND) return go2d<3, PAT_DIAMOND>(g, w, in, out, tile_rows, st);
+            return go2d<3, PAT_DENSE>(g, w, in, out, tile_rows, st);
         }
     } else if (g.dims == 3) {
         if (R == 1) {

@@ -418,15 +418,26 @@ __global__ void k_to_fp64(const float2 *__restrict__ src, double *__restrict__ d
     }
 }
 
-// Re-anchor: round each (hi, lo) through FP64 back to a normalised pair.
-__global__ void k_reanchor(float2 *__restrict__ g, long long n)
+// In-place format changes of one buffer (FP64 re-anchor sweeps): element i
+// is read and rewritten by one thread, 8 bytes either way.
+__global__ void k_split_to_fp64_inplace(unsigned long long *g, long long n)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const float2 v = g[i];
-        const double x = (double)v.x + (double)v.y;
+        const unsigned long long bits = g[i];
+        const float2 v = make_float2(__uint_as_float((unsigned)bits), __uint_as_float((unsigned)(bits >> 32)));
+        g[i] = (unsigned long long)__double_as_longlong((double)v.x + (double)v.y);
+    }
+}
+
+__global__ void k_fp64_to_split_inplace(unsigned long long *g, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double x = __longlong_as_double((long long)g[i]);
         const float hi = __double2float_rn(x);
-        g[i] = make_float2(hi, __double2float_rn(x - (double)hi));
+        const float lo = __double2float_rn(x - (double)hi);
+        g[i] = ((unsigned long long)__float_as_uint(lo) << 32) | __float_as_uint(hi);
     }
 }
 
@@ -566,10 +577,17 @@ cudaError_t launch_split_to_fp64(long long n, const float2 *src, double *dst, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_reanchor(long long n, float2 *grid, cudaStream_t st)
+cudaError_t launch_split_to_fp64_inplace(long long n, void *grid, cudaStream_t st)
 {
     note_launch();
-    k_reanchor<<<grid_for(n), 256, 0, st>>>(grid, n);
+    k_split_to_fp64_inplace<<<grid_for(n), 256, 0, st>>>((unsigned long long *)grid, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp64_to_split_inplace(long long n, void *grid, cudaStream_t st)
+{
+    note_launch();
+    k_fp64_to_split_inplace<<<grid_for(n), 256, 0, st>>>((unsigned long long *)grid, n);
     return cudaGetLastError();
 }
 

@@ -71,6 +71,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 
@@ -271,18 +272,101 @@ __device__ __forceinline__ void tile_mma(unsigned d_base, unsigned long long a0,
         tile_mma<D, I + 1, 0>(d_base, a0, b0);
 }
 
+// One grid of a batch (batch mode): its tensor map, output, sizes, tile
+// numbering and weight digits. Records live in a device array.
 template <class F>
+struct alignas(128) TcGrid {
+    CUtensorMap map;          // window map over the source buffer
+    typename F::Out *out;     // interior point (0, 0) of the destination
+    long long ld;
+    int m, n, tiles_x, tile_begin, map_x, map_y;
+    typename F::Digits digits;
+};
+
+// B_i: N row nn = NLV e + 8 rho + c (digit e of w, output row rho of the
+// group, column c of the block), K index k; threads t0, t0 + nt, ... fill it.
+template <class F>
+__device__ __forceinline__ void build_bmat(Smem<F> &S, const typename F::Digits &sw, int t0, int nt)
+{
+    constexpr int NCOL = NLV * F::kDigits;
+    for (int idx = t0; idx < NOFF * NCOL * 16; idx += nt) {
+        const int i = idx / (NCOL * 16), rem = idx - i * (NCOL * 16);
+        const int nn = rem >> 4, k = rem & 15;
+        const int e = nn / NLV, rho = (nn % NLV) >> 3, c = nn & 7;
+        const int ti = i - rho, tj = k - c - 1;
+        const __half v = (ti >= 0 && ti < 7 && tj >= 0 && tj < 7) ? sw.d[e][ti * 7 + tj] : __float2half(0.f);
+        S.bmat[i][(nn >> 3) * 128 + (nn & 7) * 8 + (k >> 3) * 64 + (k & 7)] = v;
+    }
+}
+
+// Batch mode: the grid of global tile `tile` (last record whose tile_begin
+// is not above it).
+template <class F>
+__device__ __forceinline__ int grid_of(const TcGrid<F> *grids, int ngrids, int tile)
+{
+    int lo = 0, hi = ngrids - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (grids[mid].tile_begin <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One grid (BATCH = false: kernel parameters describe it, tiles are dealt
+// round-robin) or a batch of grids (BATCH = true: `grids` describes them,
+// each CTA takes a contiguous run of the batch's tiles, and the MMA warp
+// rebuilds its B matrices when the run crosses into the next grid, after
+// the MMAs of the previous tile have completed).
+template <class F, bool BATCH>
 __global__ void __launch_bounds__(kThreads, 1)
     k2d_tc(const __grid_constant__ CUtensorMap tmap, typename F::Out *__restrict__ out, int m, int n,
-           long long ld, int tiles_x, int tiles, int map_x, int map_y, typename F::Digits sw, WaitCfg wc)
+           long long ld, int tiles_x, int tiles, int map_x, int map_y, typename F::Digits sw, WaitCfg wc,
+           const TcGrid<F> *__restrict__ grids, int ngrids)
 {
     constexpr int D = F::kDigits;
-    constexpr int NCOL = NLV * D;
     using SM = Smem<F>;
     extern __shared__ unsigned char smem_raw[];
     SM &S = *reinterpret_cast<SM *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int my_tiles = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    int my_tiles, first = 0;
+    if constexpr (BATCH) {
+        const int per = tiles / (int)gridDim.x, extra = tiles % (int)gridDim.x, b = (int)blockIdx.x;
+        first = b * per + min(b, extra);
+        my_tiles = per + (b < extra ? 1 : 0);
+    } else {
+        my_tiles = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    }
+    // Where tile `it` of this CTA lies: its grid and output origin.
+    auto tile_at = [&](int it, int &g, int &x0, int &y0) {
+        if constexpr (BATCH) {
+            const int tile = first + it;
+            g = grid_of(grids, ngrids, tile);
+            const int local = tile - grids[g].tile_begin, tx = grids[g].tiles_x;
+            const int ty = local / tx;
+            x0 = (local - ty * tx) * TX;
+            y0 = ty * TY;
+        } else {
+            const int tile = blockIdx.x + it * gridDim.x;
+            const int ty = tile / tiles_x;
+            g = 0;
+            x0 = (tile - ty * tiles_x) * TX;
+            y0 = ty * TY;
+        }
+    };
+    auto load_window = [&](int it, unsigned bar) {
+        int g, x0, y0;
+        tile_at(it, g, x0, y0);
+        const CUtensorMap *map = &tmap;
+        int mx = map_x, my = map_y;
+        if constexpr (BATCH) {
+            map = &grids[g].map;
+            mx = grids[g].map_x;
+            my = grids[g].map_y;
+        }
+        mbar_expect_tx(bar, kStageBytes);
+        tma_load_2d(smem_addr(S.stage), map, mx + x0 - 4, my + y0 - 3, bar);
+    };
     volatile int *abort = &S.abort;
     const unsigned stage_full = smem_addr(&S.stage_full), stage_empty = smem_addr(&S.stage_empty);
     auto bar2 = [](unsigned long long (&b)[2], int i) { return smem_addr(&b[i]); };
@@ -304,10 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (my_tiles > 0 && !wc.skip_loads) {  // the first window load overlaps the set-up below
-            const int ty = (int)blockIdx.x / tiles_x;
-            const int x0 = ((int)blockIdx.x - ty * tiles_x) * TX, y0 = ty * TY;
-            mbar_expect_tx(stage_full, kStageBytes);
-            tma_load_2d(smem_addr(S.stage), &tmap, map_x + x0 - 4, map_y + y0 - 3, stage_full);
+            load_window(0, stage_full);
             issued = 1;
         }
     }
@@ -317,38 +398,31 @@ __global__ void __launch_bounds__(kThreads, 1)
                      "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    // B_i: N row nn = NLV e + 8 rho + c (digit e of w, output row rho of the
-    // group, column c of the block), K index k.
-    for (int idx = tid; idx < NOFF * NCOL * 16; idx += kThreads) {
-        const int i = idx / (NCOL * 16), rem = idx - i * (NCOL * 16);
-        const int nn = rem >> 4, k = rem & 15;
-        const int e = nn / NLV, rho = (nn % NLV) >> 3, c = nn & 7;
-        const int ti = i - rho, tj = k - c - 1;
-        const __half v = (ti >= 0 && ti < 7 && tj >= 0 && tj < 7) ? sw.d[e][ti * 7 + tj] : __float2half(0.f);
-        S.bmat[i][(nn >> 3) * 128 + (nn & 7) * 8 + (k >> 3) * 64 + (k & 7)] = v;
+    // B matrices of the first tile's grid (batch mode: the MMA warp rebuilds
+    // them whenever its run of tiles enters another grid).
+    int g_bmat = 0;
+    if constexpr (BATCH) {
+        if (my_tiles > 0) {
+            int x0, y0;
+            tile_at(0, g_bmat, x0, y0);
+            build_bmat<F>(S, grids[g_bmat].digits, tid, kThreads);
+        }
+    } else {
+        build_bmat<F>(S, sw, tid, kThreads);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = S.tmem;
-    auto tile_origin = [&](int it, int &x0, int &y0) {
-        const int tile = blockIdx.x + it * gridDim.x;
-        const int ty = tile / tiles_x;
-        x0 = (tile - ty * tiles_x) * TX;
-        y0 = ty * TY;
-    };
 
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
         if (lane == 0 && !wc.skip_loads) {
             for (int it = issued; it < my_tiles; ++it) {
                 if (!wait(stage_empty, (it & 1) ^ 1)) break;
-                int x0, y0;
-                tile_origin(it, x0, y0);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(stage_full, kStageBytes);
-                tma_load_2d(smem_addr(S.stage), &tmap, map_x + x0 - 4, map_y + y0 - 3, stage_full);
+                load_window(it, stage_full);
                 issued = it + 1;
             }
         }
@@ -357,20 +431,41 @@ __global__ void __launch_bounds__(kThreads, 1)
         const unsigned long long a_desc_buf0 = smem_desc(smem_addr(S.planes[0][0]), 16, R * kRowBytes);
         const unsigned long long a_desc_buf1 = smem_desc(smem_addr(S.planes[1][0]), 16, R * kRowBytes);
         const unsigned long long b_desc0 = smem_desc(smem_addr(S.bmat[0]), 128, 256);
-        if (lane == 0) {
-            for (int it = 0; it < my_tiles; ++it) {
-                const int buf = it & 1, use = it >> 1;
-                if (!wait(bar2(S.planes_full, buf), use & 1)) break;
-                if (!wait(bar2(S.acc_empty, buf), (use & 1) ^ 1)) break;
-                tc_fence_after();
-                // The issuing thread stalls on every MMA until the tensor core
-                // takes it, so nothing else sits between them: all MMAs are
-                // unrolled, each descriptor one add of a compile-time offset.
-                tile_mma<D, 0, 0>(tmem + (unsigned)(kAccStride * buf), buf ? a_desc_buf1 : a_desc_buf0, b_desc0);
-                mma_commit(bar2(S.planes_empty, buf));  // planes may be overwritten
-                mma_commit(bar2(S.acc_full, buf));      // accumulator ready
-                committed = it + 1;
+        for (int it = 0; it < my_tiles; ++it) {
+            const int buf = it & 1, use = it >> 1;
+            if constexpr (BATCH) {
+                int g, x0, y0;
+                tile_at(it, g, x0, y0);
+                if (g != g_bmat) {
+                    // New grid: once the MMAs of the previous tile (and so all
+                    // earlier ones) are done reading B, the warp rewrites it.
+                    int ok = 1;
+                    if (lane == 0 && it > 0) ok = wait(bar2(S.acc_full, (it - 1) & 1), ((it - 1) >> 1) & 1);
+                    if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+                    tc_fence_after();
+                    build_bmat<F>(S, grids[g].digits, lane, 32);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    g_bmat = g;
+                }
             }
+            int ok = 1;
+            if (lane == 0) {
+                ok = wait(bar2(S.planes_full, buf), use & 1) && wait(bar2(S.acc_empty, buf), (use & 1) ^ 1);
+                if (ok) {
+                    tc_fence_after();
+                    // The issuing thread stalls on every MMA until the tensor
+                    // core takes it, so nothing else sits between them: all
+                    // MMAs are unrolled, each descriptor one add of a
+                    // compile-time offset.
+                    tile_mma<D, 0, 0>(tmem + (unsigned)(kAccStride * buf), buf ? a_desc_buf1 : a_desc_buf0,
+                                      b_desc0);
+                    mma_commit(bar2(S.planes_empty, buf));  // planes may be overwritten
+                    mma_commit(bar2(S.acc_full, buf));      // accumulator ready
+                    committed = it + 1;
+                }
+            }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
         }
     } else if (warp < kWarpEpi0) {
         // ------------------------------------------------ slicers
@@ -481,8 +576,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int buf = it & 1, use = it >> 1;
             if (!wait(bar2(S.acc_full, buf), use & 1)) break;
             tc_fence_after();
-            int x0, y0;
-            tile_origin(it, x0, y0);
+            int g, x0, y0;
+            tile_at(it, g, x0, y0);
+            typename F::Out *o_base = out;
+            long long o_ld = ld;
+            int o_m = m, o_n = n, ew = sw.ew;
+            if constexpr (BATCH) {
+                o_base = grids[g].out;
+                o_ld = grids[g].ld;
+                o_m = grids[g].m;
+                o_n = grids[g].n;
+                ew = grids[g].digits.ew;
+            }
             const int ex = S.scale_exp[it & 3];
             const int xb = x0 + 8 * eb;
 #pragma unroll 1
@@ -499,11 +604,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (lane == 0) mbar_arrive(bar2(S.acc_empty, buf));
                 }
                 const int yy = y0 + R * er + rho;
-                if (yy >= m) continue;
+                if (yy >= o_m) continue;
                 if constexpr (F::kF64) {
                     // value = T 2^c with T from the levels (f64_combine) and
                     // c = (input scale) + (weight scale) - 1080.
-                    const int c = ex + sw.ew - 1080;
+                    const int c = ex + ew - 1080;
                     double res[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
@@ -511,16 +616,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                         res[j] = ex == kNonFiniteTile ? __longlong_as_double(0x7FF8000000000000ll)
                                                       : f64_from_fixed(f64_combine(lv), c);
                     }
-                    double *o = reinterpret_cast<double *>(out) + (long long)yy * ld + xb;
+                    double *o = reinterpret_cast<double *>(o_base) + (long long)yy * o_ld + xb;
 #pragma unroll
                     for (int j = 0; j < 8; j += 2) {
-                        if (xb + j + 1 < n)
+                        if (xb + j + 1 < o_n)
                             *reinterpret_cast<double2 *>(o + j) = make_double2(res[j], res[j + 1]);
-                        else if (xb + j < n)
+                        else if (xb + j < o_n)
                             o[j] = res[j];
                     }
                 } else {
-                    const float scale = ldexpf(1.0f, ex + sw.ew - 2 * kDigitBits);
+                    const float scale = ldexpf(1.0f, ex + ew - 2 * kDigitBits);
                     float2 res[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
@@ -531,13 +636,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                         two_sum(h2, (e1 + e2) + tail, hi, lo);
                         res[j] = make_float2(hi * scale, lo * scale);
                     }
-                    float2 *o = reinterpret_cast<float2 *>(out) + (long long)yy * ld + xb;
+                    float2 *o = reinterpret_cast<float2 *>(o_base) + (long long)yy * o_ld + xb;
 #pragma unroll
                     for (int j = 0; j < 8; j += 2) {
-                        if (xb + j + 1 < n)
+                        if (xb + j + 1 < o_n)
                             *reinterpret_cast<float4 *>(o + j) =
                                 make_float4(res[j].x, res[j].y, res[j + 1].x, res[j + 1].y);
-                        else if (xb + j < n)
+                        else if (xb + j < o_n)
                             o[j] = res[j];
                     }
                 }
@@ -560,6 +665,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
+template <class F, bool BATCH>
+cudaError_t set_smem_attr()
+{
+    static const cudaError_t err = cudaFuncSetAttribute(k2d_tc<F, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        (int)(sizeof(Smem<F>) + 128));
+    return err;
+}
+
 template <class F>
 cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long long origin, long long elements,
                       const void *in_base, void *out_base, const WaitCfg &wc, cudaStream_t st)
@@ -570,24 +683,60 @@ cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long 
     cudaError_t e = encode_split_window_map(&map, reinterpret_cast<const float2 *>(in_base), ld, elements / ld,
                                             ST_X, ST_Y);
     if (e != cudaSuccess) return e;
-    const size_t smem = sizeof(Smem<F>) + 128;
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, [smem] {
-        attr_err = cudaFuncSetAttribute(k2d_tc<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    });
-    if (attr_err != cudaSuccess) return attr_err;
+    if ((e = set_smem_attr<F, false>()) != cudaSuccess) return e;
     const int tiles_x = (int)((g.ext[1] + TX - 1) / TX);
     const int tiles = tiles_x * (int)((g.ext[0] + TY - 1) / TY);
     // One CTA per SM (its shared-memory footprint admits no second one, so
     // the TMEM allocation never waits).
     const int grid = std::min(tiles, device_sm_count());
     note_launch();
-    k2d_tc<F><<<grid, kThreads, smem, st>>>(map, reinterpret_cast<typename F::Out *>(out_base) + origin,
-                                            (int)g.ext[0], (int)g.ext[1], ld, tiles_x, tiles, (int)(origin % ld),
-                                            (int)(origin / ld), digits, wc);
+    k2d_tc<F, false><<<grid, kThreads, sizeof(Smem<F>) + 128, st>>>(
+        map, reinterpret_cast<typename F::Out *>(out_base) + origin, (int)g.ext[0], (int)g.ext[1], ld, tiles_x,
+        tiles, (int)(origin % ld), (int)(origin / ld), digits, wc, nullptr, 0);
     return cudaGetLastError();
 }
+
+template <class F>
+cudaError_t fill_record(void *rec, const GridView &g, const Weights &w, long long origin, long long elements,
+                        const void *in_base, void *out_base, int tile_begin, int *tiles,
+                        typename F::Digits (*slice)(const Weights &))
+{
+    TcGrid<F> r;
+    std::memset(&r, 0, sizeof r);
+    const long long ld = g.pitch[0];
+    cudaError_t e = encode_split_window_map(&r.map, reinterpret_cast<const float2 *>(in_base), ld, elements / ld,
+                                            ST_X, ST_Y);
+    if (e != cudaSuccess) return e;
+    r.out = reinterpret_cast<typename F::Out *>(out_base) + origin;
+    r.ld = ld;
+    r.m = (int)g.ext[0];
+    r.n = (int)g.ext[1];
+    r.tiles_x = (int)((g.ext[1] + TX - 1) / TX);
+    r.tile_begin = tile_begin;
+    r.map_x = (int)(origin % ld);
+    r.map_y = (int)(origin / ld);
+    r.digits = slice(w);
+    *tiles = r.tiles_x * (int)((g.ext[0] + TY - 1) / TY);
+    std::memcpy(rec, &r, sizeof r);
+    return cudaSuccess;
+}
+
+template <class F>
+cudaError_t launch_batch(const void *records, int ngrids, int total, const WaitCfg &wc, cudaStream_t st)
+{
+    cudaError_t e = set_smem_attr<F, true>();
+    if (e != cudaSuccess) return e;
+    CUtensorMap unused;
+    std::memset(&unused, 0, sizeof unused);
+    const int grid = std::min(total, device_sm_count());
+    note_launch();
+    k2d_tc<F, true><<<grid, kThreads, sizeof(Smem<F>) + 128, st>>>(
+        unused, nullptr, 0, 0, 0, 0, total, 0, 0, typename F::Digits{}, wc,
+        reinterpret_cast<const TcGrid<F> *>(records), ngrids);
+    return cudaGetLastError();
+}
+
+split::SliceWeights split_digits(const Weights &w) { return split::slice_weights(w); }
 
 }  // namespace
 
@@ -604,6 +753,26 @@ cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long 
 {
     return launch_tc<FmtF64>(g, f64_slice_weights(w), origin, elements, in_base, out_base,
                              WaitCfg{wt.limit_ns, wt.skip_loads}, st);
+}
+
+size_t tc_batch_record_bytes(bool fp64) { return fp64 ? sizeof(TcGrid<FmtF64>) : sizeof(TcGrid<FmtSplit>); }
+
+cudaError_t tc_batch_fill_record(bool fp64, void *rec, const GridView &g, const Weights &w, long long origin,
+                                 long long elements, const void *in_base, void *out_base, int tile_begin,
+                                 int *tiles)
+{
+    return fp64 ? fill_record<FmtF64>(rec, g, w, origin, elements, in_base, out_base, tile_begin, tiles,
+                                      f64_slice_weights)
+                : fill_record<FmtSplit>(rec, g, w, origin, elements, in_base, out_base, tile_begin, tiles,
+                                        split_digits);
+}
+
+cudaError_t launch_tc_batch(bool fp64, const void *records, int ngrids, int total_tiles, const TcWait &wt,
+                            cudaStream_t st)
+{
+    const WaitCfg wc{wt.limit_ns, wt.skip_loads};
+    return fp64 ? launch_batch<FmtF64>(records, ngrids, total_tiles, wc, st)
+                : launch_batch<FmtSplit>(records, ngrids, total_tiles, wc, st);
 }
 
 cudaError_t split_tc_wait_timeouts(unsigned *count, bool reset)

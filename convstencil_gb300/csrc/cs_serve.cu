@@ -37,6 +37,11 @@
 #include <thread>
 #include <vector>
 
+namespace cs {
+cs_status run_from(cs_plan *p, void *a, void *b, long long first_sweep, long long steps, cudaStream_t st,
+                   int *result_in_b);
+}  // namespace cs
+
 namespace {
 
 // Requests below this many tap-updates (about 4 ms of FP64 FMA work) are
@@ -198,21 +203,16 @@ bool start_request(cs_server *s, Request *r)
     return true;
 }
 
-// Issues `steps` steps of r on its stream, re-anchoring split grids through
-// FP64 whenever the request's global step count crosses a multiple of 100.
+// Issues `steps` steps of r on its stream. The sweeps are numbered from the
+// request's start, so split grids take their FP64 re-anchor sweeps at the
+// same global sweep counts however the run is chunked.
 cs_status issue_steps(Request *r, long long steps)
 {
     int in_b = 0;
-    cs_status st = cs_run(r->plan, r->d[r->cur], r->d[r->cur ^ 1], steps, r->stream, &in_b);
+    cs_status st = cs::run_from(r->plan, r->d[r->cur], r->d[r->cur ^ 1], r->issued / r->sweeps_per_step, steps,
+                                r->stream, &in_b);
     if (st != CS_OK) return st;
     r->cur ^= in_b;
-    if (r->prec == CS_PREC_SPLIT) {
-        const long long before = r->issued / r->sweeps_per_step / 100;
-        const long long after = (r->issued + steps) / r->sweeps_per_step / 100;
-        if (after != before &&
-            cs::launch_split_reanchor(r->layout.elements, (float2 *)r->d[r->cur], r->stream) != cudaSuccess)
-            return CS_ERR_CUDA;
-    }
     return CS_OK;
 }
 
@@ -495,7 +495,6 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
               cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_TC) == CS_OK))
             cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_FMA);
     }
-    cs_plan_set_option(r->plan, CS_OPT_REANCHOR_INTERVAL, 0);  // the server re-anchors at global steps
     long long sweeps1 = 0;
     if (d->semantics == CS_SEM_FUSED) {
         for (long long k = 1; k <= 3; ++k)

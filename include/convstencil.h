@@ -105,11 +105,17 @@ typedef enum cs_algo {
 
 typedef enum cs_option {
     CS_OPT_ALGO = 0,              /* cs_algo */
-    CS_OPT_REANCHOR_INTERVAL = 2, /* split: renormalise (hi,lo) through FP64 every N
-                                     sweeps (default 100, 0 = never) */
+    CS_OPT_REANCHOR_INTERVAL = 2, /* split: every N-th sweep is an FP64 re-anchor sweep,
+                                     computed in FP64 arithmetic from the (hi, lo) state
+                                     (converted in place, no allocation; the tcgen05 FP64
+                                     pipeline for 2D radius-3 plans, FP64 FMA otherwise);
+                                     sweeps are counted from the start of the run
+                                     (default 100, 0 = never) */
     CS_OPT_TIME_BLOCK = 3,        /* split double-float kernels, 2D radius 1 and 1D:
                                      steps fused per launch by temporal blocking
                                      (0 = tuner picks 1..4, default; 1 = off) */
+    CS_OPT_TILE_ROWS = 6,         /* FP64 FMA 2D kernel: rows per CTA tile, 16 or 32 (0 = tuner,
+                                     default: the first run times both; results do not depend on it) */
     CS_OPT_WAIT_LIMIT_US = 4,     /* bound of each device-side wait of the tcgen05 kernels, in
                                      microseconds (default 2,000,000; 1 .. 60,000,000) */
     CS_OPT_WAIT_TEST_SKIP_LOADS = 5 /* test hook (0/1): the tcgen05 kernels issue no TMA loads,
@@ -154,6 +160,9 @@ CS_API cs_status cs_plan_sweeps(const cs_plan *plan, long long steps, long long 
 CS_API cs_status cs_plan_get_algo(const cs_plan *plan, int *algo);
 /* Steps per launch the plan's last cs_run used (temporal blocking; 1 = off). */
 CS_API cs_status cs_plan_get_time_block(const cs_plan *plan, int *steps_per_launch);
+/* Rows per CTA tile of the FP64 FMA 2D kernel in the plan's last cs_run
+ * (the tuner's choice under 0; 0 when another kernel ran). */
+CS_API cs_status cs_plan_get_tile_rows(const cs_plan *plan, int *rows);
 CS_API cs_status cs_plan_destroy(cs_plan *plan);
 
 /* Runs `steps` steps from buffer a, ping-ponging with b (both per the plan's

@@ -65,9 +65,11 @@ def test_graph_blocks_bitwise_equal_plain_launches(shape, ext, prec):
 
 
 def test_graph_blocks_keep_reanchor_points():
-    """Re-anchoring at every 40th sweep inside a long run: graph blocks are
-    used only where no re-anchor falls inside them; the result equals the
-    same run with graphs impossible (large chunks never reach 3 blocks)."""
+    """FP64 re-anchor sweeps at every 64th sweep inside a long run: graph
+    blocks are used only where no re-anchor sweep falls inside them; the
+    result equals the same sweeps done one call at a time, with each 64th
+    sweep run by hand as an FP64 sweep (FP64 conversion, one FP64 tcgen05
+    sweep, conversion back)."""
     cs.build()
     ext = (192, 256)
     w = O.seeded_weights(49, 42)
@@ -75,19 +77,24 @@ def test_graph_blocks_keep_reanchor_points():
     p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
     p.set_option(cs.Option.REANCHOR_INTERVAL, 64)
     ref = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
-    ref.set_option(cs.Option.REANCHOR_INTERVAL, 64)
+    ref.set_option(cs.Option.REANCHOR_INTERVAL, 0)
+    p64 = cs.Plan("box2d3r", ext, w)
+    p64.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
     p.run(_start(p, x), torch.zeros_like(_start(p, x)), 4)
     ref.set_option(cs.Option.ALGO, p.algo)
     got = _run(p, x, 256, 256)
-    # the same sweeps one launch per call, re-anchoring by hand at 64, 128, ...
     a = _start(ref, x)
     b = torch.zeros_like(a)
     bufs, cur = [a, b], 0
-    raw = torch.zeros(ref.elements, dtype=torch.float64, device="cuda")
+    r0 = torch.zeros(ref.elements, dtype=torch.float64, device="cuda")
+    r1 = torch.zeros_like(r0)
     for i in range(256):
-        cur ^= ref.run(bufs[cur], bufs[cur ^ 1], 1)
         if (i + 1) % 64 == 0:
-            ref.split_to_fp64(bufs[cur], raw)
-            ref.split_from_fp64(raw, bufs[cur])
+            ref.split_to_fp64(bufs[cur], r0)
+            p64.run(r0, r1, 1)
+            ref.split_from_fp64(r1, bufs[cur ^ 1])
+            cur ^= 1
+        else:
+            cur ^= ref.run(bufs[cur], bufs[cur ^ 1], 1)
     torch.cuda.synchronize()
     assert np.array_equal(got, bufs[cur].cpu().numpy())

@@ -185,3 +185,27 @@ def test_zero_steps_and_launch_counter():
     np.testing.assert_array_equal(out, x)
     p.run_host(x, 3)
     assert cs.kernel_launch_count() - before >= 3
+
+
+def test_fp64_tile_rows_do_not_change_results():
+    """The FP64 FMA 2D kernel's 16- and 32-row tiles (the tuner's choice per
+    size class) sum every point's taps in the same order: bitwise equal."""
+    torch = pytest.importorskip("torch")
+    ext = (300, 260)
+    w = O.seeded_weights(5, 31)
+    x = O.splitmix_uniform(ext[0] * ext[1], 32).reshape(ext)
+    outs = []
+    for rows in (16, 32, 0):
+        p = cs.Plan("star2d1r", ext, w)
+        p.set_option(cs.Option.ALGO, cs.Algo.FP64_FMA)
+        p.set_option(cs.Option.TILE_ROWS, rows)
+        a = torch.from_numpy(p.pack(x)).cuda()
+        b = torch.zeros_like(a)
+        in_b = p.run(a, b, 7)
+        torch.cuda.synchronize()
+        outs.append((b if in_b else a).cpu().numpy())
+        assert p.tile_rows == (rows or p.tile_rows) and p.tile_rows in (16, 32)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+    with pytest.raises(cs.ConvStencilError):
+        cs.Plan("star2d1r", ext, w).set_option(cs.Option.TILE_ROWS, 8)

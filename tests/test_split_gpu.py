@@ -122,17 +122,29 @@ def test_split_signed_weights_and_wide_range():
         assert rel_err(p.unpack(got), p.unpack(ref))[1] <= TOL
 
 
-def test_split_long_run_with_reanchor():
-    ext = (128, 192)
-    w = O.seeded_weights(49, 21)
-    p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
-    p.set_option(cs.Option.REANCHOR_INTERVAL, 25)
-    x = O.splitmix_uniform(ext[0] * ext[1], 22).reshape(ext)
-    buf = p.pack(x)
-    got = split_run(p, buf, 200)
-    ref = oracle_run(p, buf, w, 3, 200)
-    err = rel_err(p.unpack(got), p.unpack(ref))
-    assert err[1] <= TOL and err[0] <= 1e-8, err
+@pytest.mark.parametrize("shape,ext,algo", [("box2d3r", (256, 320), cs.Algo.SPLIT_TC),
+                                             ("box3d1r", (64, 64, 72), cs.Algo.SPLIT_TC),
+                                             ("box3d1r", (40, 48, 56), cs.Algo.SPLIT_FMA)])
+def test_split_long_run_with_fp64_reanchor(shape, ext, algo):
+    """200 steps with and without FP64 re-anchor sweeps (one sweep in every
+    100 computed in FP64 from the (hi, lo) state): both within the 1e-10
+    pointwise bar against the oracle, and the re-anchored run differs from
+    the plain one (the FP64 sweeps really run)."""
+    info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
+    w = O.seeded_weights(info[1], 21)
+    x = O.splitmix_uniform(int(np.prod(ext)), 22).reshape(ext)
+    got = {}
+    for interval in (0, 100):
+        p = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT)
+        p.set_option(cs.Option.ALGO, algo)
+        p.set_option(cs.Option.REANCHOR_INTERVAL, interval)
+        buf = p.pack(x)
+        got[interval] = split_run(p, buf, 200)
+    ref = oracle_run(p, buf, w, info[4], 200)
+    for interval, g in got.items():
+        err = rel_err(p.unpack(g), p.unpack(ref))
+        assert err[0] <= TOL, (interval, err)
+    assert not np.array_equal(got[0], got[100])
 
 
 def test_split_roundtrip_conversion():
