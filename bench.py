@@ -808,8 +808,9 @@ def main():
             e2e = {"value": round(world * pts * K / te / 1e9, 4), "unit": "GStencil/s",
                    "h2d_bytes_per_step": round(gbytes / K, 1), "d2h_bytes_per_step": round(gbytes / K, 1),
                    "note": f"cs_run_host: one {gbytes / 1e6:.0f} MB FP64 host->device and device->host copy per "
-                           f"{K}-step run, pinned host buffers, allocation and FP64<->(hi, lo) conversion "
-                           "included; median of 3 complete calls",
+                           f"{K}-step run, pinned host buffers, FP64<->(hi, lo) conversion included; the plan "
+                           "allocates its two device grids on its first call and keeps them (the first call "
+                           "below includes that allocation); median of 3 complete calls",
                    "calls_ms": [round(t * 1e3, 2) for t in times]}
             del pin_in, pin_out
         if "fp64" in results:

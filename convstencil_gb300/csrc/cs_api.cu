@@ -234,10 +234,18 @@ struct cs_plan {
     std::mutex graph_mu;
     std::map<std::tuple<const void *, const void *, int, int, int>, cudaGraphExec_t> graphs;
     cudaStream_t capture_stream = nullptr;
+    // Host-buffer runs (cs_run_host): the two device grids, allocated by the
+    // first call and kept for later ones; a call that finds them in use by
+    // another thread allocates its own.
+    std::mutex host_mu;
+    void *host_bufs[2] = {nullptr, nullptr};
+    size_t host_bytes = 0;
     ~cs_plan()
     {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
         if (capture_stream) cudaStreamDestroy(capture_stream);
+        for (void *b : host_bufs)
+            if (b) cudaFree(b);
     }
 };
 
@@ -922,23 +930,36 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
     if (s != CS_OK) return s;
     const size_t bytes = p->layout.bytes;
     const size_t elem_bytes = sizeof(double);
-    DevBuf d[2], stage;
-    // Buffers the copy (or the conversion of a whole copied grid) fills
-    // completely need no clearing; the second buffer's halo must be zero.
-    const bool whole = in_elems * elem_bytes == bytes;
-    CS_CUDA(cudaMalloc(&d[0].p, bytes));
-    CS_CUDA(cudaMalloc(&d[1].p, bytes));
-    if (!whole) CS_CUDA(cudaMemset(d[0].p, 0, bytes));
-    CS_CUDA(cudaMemset(d[1].p, 0, bytes));
-    if (p->prec == CS_PREC_FP64) {
-        CS_CUDA(cudaMemcpy(d[0].p, host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
+    const long long n = p->layout.elements;
+    // Two device grids: the plan's kept pair when no other thread holds it.
+    std::unique_lock<std::mutex> kept(p->host_mu, std::try_to_lock);
+    DevBuf own[2];
+    void *d[2];
+    if (kept.owns_lock()) {
+        if (p->host_bytes < bytes) {
+            for (void *&b : p->host_bufs)
+                if (b) cudaFree(b), b = nullptr;
+            p->host_bytes = 0;
+            CS_CUDA(cudaMalloc(&p->host_bufs[0], bytes));
+            CS_CUDA(cudaMalloc(&p->host_bufs[1], bytes));
+            p->host_bytes = bytes;
+        }
+        d[0] = p->host_bufs[0];
+        d[1] = p->host_bufs[1];
     } else {
-        CS_CUDA(cudaMalloc(&stage.p, bytes));
-        if (!whole) CS_CUDA(cudaMemset(stage.p, 0, bytes));
-        CS_CUDA(cudaMemcpy(stage.p, host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
-        s = cs_split_from_fp64(p, (const double *)stage.p, d[0].p, nullptr);
-        if (s != CS_OK) return s;
+        CS_CUDA(cudaMalloc(&own[0].p, bytes));
+        CS_CUDA(cudaMalloc(&own[1].p, bytes));
+        d[0] = own[0].p;
+        d[1] = own[1].p;
     }
+    // The copy fills the first grid completely unless the caller passes a
+    // part of it; the second grid's halo must read as zero. A split plan's
+    // grid is converted from FP64 in place (same 8 bytes per point).
+    const bool whole = in_elems * elem_bytes == bytes;
+    if (!whole) CS_CUDA(cudaMemset(d[0], 0, bytes));
+    CS_CUDA(cudaMemset(d[1], 0, bytes));
+    CS_CUDA(cudaMemcpy(d[0], host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
+    if (p->prec == CS_PREC_SPLIT) CS_CUDA(cs::launch_fp64_to_split_inplace(n, d[0], nullptr));
     // Bounded device-side waits that expire during this call leave outputs
     // unwritten; the counters before and after tell (any expiry in the
     // process during the call counts).
@@ -950,7 +971,7 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
     CS_CUDA(cudaEventCreate(&e1));
     CS_CUDA(cudaEventRecord(e0, nullptr));
     int in_b = 0;
-    s = cs_run(p, d[0].p, d[1].p, steps, nullptr, &in_b);
+    s = cs_run(p, d[0], d[1], steps, nullptr, &in_b);
     if (s != CS_OK) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -969,12 +990,8 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
     if (waits_after != waits_before)
         return fail(CS_ERR_TIMEOUT, "%u bounded device-side wait(s) expired during the run; the result is incomplete",
                     waits_after - waits_before);
-    const void *res = d[in_b].p;
-    if (p->prec == CS_PREC_SPLIT) {
-        s = cs_split_to_fp64(p, res, (double *)stage.p, nullptr);
-        if (s != CS_OK) return s;
-        res = stage.p;
-    }
+    void *res = d[in_b];
+    if (p->prec == CS_PREC_SPLIT) CS_CUDA(cs::launch_split_to_fp64_inplace(n, res, nullptr));
     CS_CUDA(cudaMemcpy(host_out, (const double *)res + out_offset, out_elems * elem_bytes,
                        cudaMemcpyDeviceToHost));
     return CS_OK;

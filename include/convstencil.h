@@ -199,10 +199,13 @@ CS_API cs_status cs_run_noalloc(cs_plan *plan, const void *in, void *out, long l
 CS_API cs_status cs_split_from_fp64(const cs_plan *plan, const double *src, void *dst, void *stream);
 CS_API cs_status cs_split_to_fp64(const cs_plan *plan, const void *src, double *dst, void *stream);
 
-/* Host-buffer form of cs_run: allocates two device grids, copies host_in
- * (FP64, plan layout) in, runs, copies the result (FP64) to host_out,
- * releases everything. Synchronous. Returns CS_ERR_TIMEOUT (result
- * incomplete) if a bounded device-side wait expired during the call. */
+/* Host-buffer form of cs_run: copies host_in (FP64, plan layout) into a
+ * device grid (converted to (hi, lo) in place for split plans), runs, copies
+ * the result (FP64) to host_out. Synchronous. The two device grids are
+ * allocated by the plan's first call and kept for its later calls until
+ * cs_plan_destroy (a call that finds them in use by another thread allocates
+ * and frees its own). Returns CS_ERR_TIMEOUT (result incomplete) if a
+ * bounded device-side wait expired during the call. */
 CS_API cs_status cs_run_host(cs_plan *plan, const double *host_in, double *host_out,
                              long long steps);
 
