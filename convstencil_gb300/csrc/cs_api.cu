@@ -10,6 +10,7 @@
 // kernels index their tiles directly), and every failure is a status code.
 #include "../../include/convstencil.h"
 #include "cs_internal.h"
+#include "cs_plan_internal.h"
 
 #include <algorithm>
 #include <atomic>
@@ -1234,14 +1235,6 @@ cs_status run_into(cs_plan *p, const void *in, void *out, void *scratch, long lo
 
 cs_status set_error(cs_status s, const char *msg) { return fail(s, "%s", msg); }
 
-struct PlanFacts {
-    int dims, radius, pattern, steps_per_sweep;
-    cs_precision prec;
-    GridView view;
-    long long origin, elements;
-    const Weights *w;
-};
-
 bool plan_facts(const cs_plan *p, PlanFacts *f)
 {
     if (!p || !f) return false;
@@ -1253,6 +1246,7 @@ bool plan_facts(const cs_plan *p, PlanFacts *f)
     f->view = p->view;
     f->origin = p->layout.origin;
     f->elements = p->layout.elements;
+    f->reanchor = p->reanchor;
     f->w = &p->w;
     return true;
 }

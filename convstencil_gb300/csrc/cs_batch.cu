@@ -18,28 +18,15 @@
 // later calls.
 #include "../../include/convstencil.h"
 #include "cs_internal.h"
+#include "cs_plan_internal.h"
 #include "cs_split_ff.cuh"
 
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <type_traits>
 #include <vector>
 
-struct cs_plan;
-
-namespace cs {
-
-struct PlanFacts {  // read-only view of a plan for the batcher (cs_api.cu)
-    int dims, radius, pattern, steps_per_sweep;
-    cs_precision prec;
-    GridView view;
-    long long origin, elements;
-    const Weights *w;
-};
-bool plan_facts(const cs_plan *p, PlanFacts *f);
-cs_status set_error(cs_status s, const char *msg);
-
-}  // namespace cs
 
 namespace {
 
@@ -53,6 +40,7 @@ struct Item {
     void *out;       // interior point (0, 0) of the destination grid
     long long ld;
     int m, n, tiles_x, tile_begin;
+    long long sweeps;  // sweeps this grid takes (launches for later sweeps skip its tiles)
 };
 
 constexpr int TX = 64, TY = 32, RPT = 8;
@@ -74,7 +62,7 @@ __device__ __forceinline__ int find_item(const It *items, int nitems, int tile)
 // FP64 FMA, the k2d_fma<R,P> body with weights from shared memory.
 template <int R, int P>
 __global__ void __launch_bounds__(256) k2d_fma_batch(const Item *__restrict__ items, int nitems,
-                                                     const double *__restrict__ wtab, int total)
+                                                     const double *__restrict__ wtab, int total, long long sweep)
 {
     constexpr int K = 2 * R + 1, SX = TX + 2 * R, SY = TY + 2 * R;
     __shared__ double s[SY * SX];
@@ -83,6 +71,7 @@ __global__ void __launch_bounds__(256) k2d_fma_batch(const Item *__restrict__ it
     for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
         const int it = find_item(items, nitems, tile);
         const Item I = items[it];
+        if (sweep >= I.sweeps) continue;  // this grid is done (uniform over the CTA)
         const int local = tile - I.tile_begin, ty = local / I.tiles_x;
         const int x0 = (local - ty * I.tiles_x) * TX, y0 = ty * TY;
         const double *in = (const double *)I.in;
@@ -128,7 +117,7 @@ __global__ void __launch_bounds__(256) k2d_fma_batch(const Item *__restrict__ it
 // Split precision, double-float on FP32 cores: the k2d_ff<R,P> body.
 template <int R, int P>
 __global__ void __launch_bounds__(256) k2d_ff_batch(const Item *__restrict__ items, int nitems,
-                                                    const float2 *__restrict__ wtab, int total)
+                                                    const float2 *__restrict__ wtab, int total, long long sweep)
 {
     constexpr int K = 2 * R + 1, SX = TX + 2 * R, SY = TY + 2 * R;
     __shared__ float2 s[SY * SX];
@@ -137,6 +126,7 @@ __global__ void __launch_bounds__(256) k2d_ff_batch(const Item *__restrict__ ite
     for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
         const int it = find_item(items, nitems, tile);
         const Item I = items[it];
+        if (sweep >= I.sweeps) continue;  // this grid is done (uniform over the CTA)
         const int local = tile - I.tile_begin, ty = local / I.tiles_x;
         const int x0 = (local - ty * I.tiles_x) * TX, y0 = ty * TY;
         const float2 *in = (const float2 *)I.in;
@@ -193,6 +183,7 @@ struct Item3 {
     void *out;
     long long ldy, ldz;
     int h, m, n, tiles_x, tiles_y, zc, tile_begin;
+    long long sweeps;  // sweeps this grid takes (launches for later sweeps skip its tiles)
 };
 
 constexpr int TX3 = 32, TY3 = 16, ZC3 = 8;
@@ -208,7 +199,7 @@ constexpr int k3d_batch_smem(bool split)
 // order from zero, weights from shared memory.
 template <int R, int P, bool SPLIT>
 __global__ void __launch_bounds__(256) k3d_batch(const Item3 *__restrict__ items, int nitems,
-                                                 const void *__restrict__ wtab, int total)
+                                                 const void *__restrict__ wtab, int total, long long sweep)
 {
     using T = typename std::conditional<SPLIT, float2, double>::type;
     constexpr int K = 2 * R + 1, SX = TX3 + 2 * R, SY = TY3 + 2 * R, PL = SX * SY, KK = K * K * K;
@@ -220,6 +211,7 @@ __global__ void __launch_bounds__(256) k3d_batch(const Item3 *__restrict__ items
     for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
         const int it = find_item(items, nitems, unit);
         const Item3 I = items[it];
+        if (sweep >= I.sweeps) continue;  // this grid is done (uniform over the CTA)
         const int local = unit - I.tile_begin, txy = I.tiles_x * I.tiles_y;
         const int tz = local / txy, rem = local - tz * txy, ty = rem / I.tiles_x;
         const int x0 = (rem - ty * I.tiles_x) * TX3, y0 = ty * TY3, z0 = tz * I.zc;
@@ -299,39 +291,40 @@ int persistent_grid(KernelT kernel, int total)
 
 template <int R, int P>
 cudaError_t launch_batch(bool split, const Item *items, int nitems, const void *wtab, int total,
-                         cudaStream_t st)
+                         long long sweep, cudaStream_t st)
 {
     cs::note_launch();
     if (split) {
         const int grid = persistent_grid(k2d_ff_batch<R, P>, total);
-        k2d_ff_batch<R, P><<<grid, 256, 0, st>>>(items, nitems, (const float2 *)wtab, total);
+        k2d_ff_batch<R, P><<<grid, 256, 0, st>>>(items, nitems, (const float2 *)wtab, total, sweep);
     } else {
         const int grid = persistent_grid(k2d_fma_batch<R, P>, total);
-        k2d_fma_batch<R, P><<<grid, 256, 0, st>>>(items, nitems, (const double *)wtab, total);
+        k2d_fma_batch<R, P><<<grid, 256, 0, st>>>(items, nitems, (const double *)wtab, total, sweep);
     }
     return cudaGetLastError();
 }
 
 cudaError_t dispatch(int R, int P, bool split, const Item *items, int nitems, const void *wtab, int total,
-                     cudaStream_t st)
+                     long long sweep, cudaStream_t st)
 {
-    if (R == 1) return P == PAT_STAR ? launch_batch<1, PAT_STAR>(split, items, nitems, wtab, total, st)
-                                     : launch_batch<1, PAT_DENSE>(split, items, nitems, wtab, total, st);
+    if (R == 1) return P == PAT_STAR ? launch_batch<1, PAT_STAR>(split, items, nitems, wtab, total, sweep, st)
+                                     : launch_batch<1, PAT_DENSE>(split, items, nitems, wtab, total, sweep, st);
     if (R == 2) {
-        if (P == PAT_STAR) return launch_batch<2, PAT_STAR>(split, items, nitems, wtab, total, st);
-        if (P == PAT_DIAMOND) return launch_batch<2, PAT_DIAMOND>(split, items, nitems, wtab, total, st);
-        return launch_batch<2, PAT_DENSE>(split, items, nitems, wtab, total, st);
+        if (P == PAT_STAR) return launch_batch<2, PAT_STAR>(split, items, nitems, wtab, total, sweep, st);
+        if (P == PAT_DIAMOND) return launch_batch<2, PAT_DIAMOND>(split, items, nitems, wtab, total, sweep, st);
+        return launch_batch<2, PAT_DENSE>(split, items, nitems, wtab, total, sweep, st);
     }
     if (R == 3) {
-        if (P == PAT_STAR) return launch_batch<3, PAT_STAR>(split, items, nitems, wtab, total, st);
-        if (P == PAT_DIAMOND) return launch_batch<3, PAT_DIAMOND>(split, items, nitems, wtab, total, st);
-        return launch_batch<3, PAT_DENSE>(split, items, nitems, wtab, total, st);
+        if (P == PAT_STAR) return launch_batch<3, PAT_STAR>(split, items, nitems, wtab, total, sweep, st);
+        if (P == PAT_DIAMOND) return launch_batch<3, PAT_DIAMOND>(split, items, nitems, wtab, total, sweep, st);
+        return launch_batch<3, PAT_DENSE>(split, items, nitems, wtab, total, sweep, st);
     }
     return cudaErrorInvalidValue;
 }
 
 template <int R, int P, bool SPLIT>
-cudaError_t launch_batch3(const Item3 *items, int nitems, const void *wtab, int total, cudaStream_t st)
+cudaError_t launch_batch3(const Item3 *items, int nitems, const void *wtab, int total, long long sweep,
+                          cudaStream_t st)
 {
     constexpr int smem = k3d_batch_smem<R>(SPLIT);
     static const cudaError_t attr =
@@ -343,28 +336,29 @@ cudaError_t launch_batch3(const Item3 *items, int nitems, const void *wtab, int 
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k3d_batch<R, P, SPLIT>, 256, smem);
     const int grid = std::max(1, std::min(total, sms * std::max(1, per)));
     cs::note_launch();
-    k3d_batch<R, P, SPLIT><<<grid, 256, smem, st>>>(items, nitems, wtab, total);
+    k3d_batch<R, P, SPLIT><<<grid, 256, smem, st>>>(items, nitems, wtab, total, sweep);
     return cudaGetLastError();
 }
 
 template <bool SPLIT>
-cudaError_t dispatch3s(int R, int P, const Item3 *items, int nitems, const void *wtab, int total, cudaStream_t st)
+cudaError_t dispatch3s(int R, int P, const Item3 *items, int nitems, const void *wtab, int total, long long sweep,
+                       cudaStream_t st)
 {
-    if (R == 1) return P == PAT_STAR ? launch_batch3<1, PAT_STAR, SPLIT>(items, nitems, wtab, total, st)
-                                     : launch_batch3<1, PAT_DENSE, SPLIT>(items, nitems, wtab, total, st);
+    if (R == 1) return P == PAT_STAR ? launch_batch3<1, PAT_STAR, SPLIT>(items, nitems, wtab, total, sweep, st)
+                                     : launch_batch3<1, PAT_DENSE, SPLIT>(items, nitems, wtab, total, sweep, st);
     if (R == 3) {
-        if (P == PAT_STAR) return launch_batch3<3, PAT_STAR, SPLIT>(items, nitems, wtab, total, st);
-        if (P == PAT_DIAMOND) return launch_batch3<3, PAT_DIAMOND, SPLIT>(items, nitems, wtab, total, st);
-        return launch_batch3<3, PAT_DENSE, SPLIT>(items, nitems, wtab, total, st);
+        if (P == PAT_STAR) return launch_batch3<3, PAT_STAR, SPLIT>(items, nitems, wtab, total, sweep, st);
+        if (P == PAT_DIAMOND) return launch_batch3<3, PAT_DIAMOND, SPLIT>(items, nitems, wtab, total, sweep, st);
+        return launch_batch3<3, PAT_DENSE, SPLIT>(items, nitems, wtab, total, sweep, st);
     }
     return cudaErrorInvalidValue;
 }
 
 cudaError_t dispatch3(int R, int P, bool split, const Item3 *items, int nitems, const void *wtab, int total,
-                      cudaStream_t st)
+                      long long sweep, cudaStream_t st)
 {
-    return split ? dispatch3s<true>(R, P, items, nitems, wtab, total, st)
-                 : dispatch3s<false>(R, P, items, nitems, wtab, total, st);
+    return split ? dispatch3s<true>(R, P, items, nitems, wtab, total, sweep, st)
+                 : dispatch3s<false>(R, P, items, nitems, wtab, total, sweep, st);
 }
 
 }  // namespace
@@ -378,12 +372,34 @@ struct cs_batch {
     void *d_w = nullptr;
     std::map<long long, cudaGraphExec_t> graphs;  // (sweeps, starting parity) -> graph
     int parity = 0;  // which buffer holds the current state of every grid
+    cudaStream_t mem_stream = nullptr;  // tables allocated and freed in order on it (server packs)
+    bool stream_mem = false;
 };
 
-extern "C" {
+namespace {
 
-CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *const *a, void *const *b,
-                                 int count)
+cudaError_t table_alloc(cs_batch *bt, void **p, size_t bytes)
+{
+    return bt->stream_mem ? cudaMallocAsync(p, bytes, bt->mem_stream) : cudaMalloc(p, bytes);
+}
+
+cudaError_t table_copy(cs_batch *bt, void *dst, const void *src, size_t bytes)
+{
+    // Stream-ordered tables come from pageable host vectors: the copy is
+    // staged before cudaMemcpyAsync returns, so the vectors may go away.
+    return bt->stream_mem ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, bt->mem_stream)
+                          : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+}
+
+}  // namespace
+
+namespace cs {
+
+// cs_batch_create with per-grid sweep counts (NULL: unbounded), the tcgen05
+// path optional, and tables allocated in order on `mem_stream` when it is not
+// NULL (no device-wide synchronisation; the server's packs).
+cs_status batch_create_ex(cs_batch **out, cs_plan *const *plans, void *const *a, void *const *b, int count,
+                          const long long *sweeps, bool allow_tc, cudaStream_t mem_stream)
 {
     if (!out || !plans || !a || !b || count < 1)
         return cs::set_error(CS_ERR_INVALID_ARGUMENT, "NULL argument or empty batch");
@@ -406,6 +422,8 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
                                  "sweep");
     }
     auto *bt = new cs_batch();
+    bt->mem_stream = mem_stream;
+    bt->stream_mem = mem_stream != nullptr;
     bt->count = count;
     bt->dims = f[0].dims;
     bt->radius = f[0].radius;
@@ -414,7 +432,7 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
     bt->split = f[0].prec == CS_PREC_SPLIT;
     // 2D radius-3 grids of at least 8 x 8 on TMA-compatible layouts and
     // 16-byte aligned buffers run on the tcgen05 kernels (split or FP64).
-    bt->tc = bt->dims == 2 && bt->radius == 3;
+    bt->tc = allow_tc && !sweeps && bt->dims == 2 && bt->radius == 3;
     for (int i = 0; bt->tc && i < count; ++i)
         bt->tc = f[i].view.ext[0] >= 8 && f[i].view.ext[1] >= 8 &&
                  cs::split_tma_layout_ok(f[i].view, f[i].origin, a[i]) &&
@@ -436,8 +454,8 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
             total += tiles;
         }
         for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
-            e = cudaMalloc(&bt->d_items[p], rb * count);
-            if (e == cudaSuccess) e = cudaMemcpy(bt->d_items[p], rec[p].data(), rb * count, cudaMemcpyHostToDevice);
+            e = table_alloc(bt, &bt->d_items[p], rb * count);
+            if (e == cudaSuccess) e = table_copy(bt, bt->d_items[p], rec[p].data(), rb * count);
         }
         bt->total = total;
         if (e != cudaSuccess) {
@@ -465,6 +483,7 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
             it.n = (int)g.ext[1];
             it.tiles_x = (int)((g.ext[1] + TX - 1) / TX);
             it.tile_begin = total;
+            it.sweeps = sweeps ? sweeps[i] : LLONG_MAX;
             total += it.tiles_x * (int)((g.ext[0] + TY - 1) / TY);
             it.in = pa;
             it.out = pb;
@@ -483,6 +502,7 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
             it.tiles_y = (int)((g.ext[1] + TY3 - 1) / TY3);
             it.zc = (int)std::min<long long>(ZC3, g.ext[0]);
             it.tile_begin = total;
+            it.sweeps = sweeps ? sweeps[i] : LLONG_MAX;
             total += it.tiles_x * it.tiles_y * (int)((g.ext[0] + it.zc - 1) / it.zc);
             it.in = pa;
             it.out = pb;
@@ -502,15 +522,14 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
     const size_t isz = bt->dims == 2 ? sizeof(Item) : sizeof(Item3);
     cudaError_t e = cudaSuccess;
     for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
-        e = cudaMalloc(&bt->d_items[p], isz * count);
+        e = table_alloc(bt, &bt->d_items[p], isz * count);
         const void *src = bt->dims == 2 ? (const void *)items[p].data() : (const void *)items3[p].data();
-        if (e == cudaSuccess) e = cudaMemcpy(bt->d_items[p], src, isz * count, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = table_copy(bt, bt->d_items[p], src, isz * count);
     }
     const size_t wbytes = bt->split ? wf.size() * sizeof(float2) : wd.size() * sizeof(double);
-    if (e == cudaSuccess) e = cudaMalloc(&bt->d_w, wbytes);
+    if (e == cudaSuccess) e = table_alloc(bt, &bt->d_w, wbytes);
     if (e == cudaSuccess)
-        e = cudaMemcpy(bt->d_w, bt->split ? (const void *)wf.data() : (const void *)wd.data(), wbytes,
-                       cudaMemcpyHostToDevice);
+        e = table_copy(bt, bt->d_w, bt->split ? (const void *)wf.data() : (const void *)wd.data(), wbytes);
     if (e != cudaSuccess) {
         cs_batch_destroy(bt);
         return cs::set_error(e == cudaErrorMemoryAllocation ? CS_ERR_OUT_OF_MEMORY : CS_ERR_CUDA,
@@ -518,6 +537,32 @@ CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *co
     }
     *out = bt;
     return CS_OK;
+}
+
+// One launch of sweep `sweep` for every grid with more sweeps than that
+// (buffer parity sweep % 2: a -> b for even sweeps). Grids past their sweep
+// count keep their state where their last sweep left it.
+cs_status batch_sweep(cs_batch *bt, long long sweep, cudaStream_t st)
+{
+    const int par = (int)(sweep & 1);
+    cudaError_t e =
+        bt->tc ? cs::launch_tc_batch(!bt->split, bt->d_items[par], bt->count, bt->total, bt->wait, st)
+        : bt->dims == 2 ? dispatch(bt->radius, bt->pattern, bt->split, (const Item *)bt->d_items[par], bt->count,
+                                   bt->d_w, bt->total, sweep, st)
+                        : dispatch3(bt->radius, bt->pattern, bt->split, (const Item3 *)bt->d_items[par], bt->count,
+                                    bt->d_w, bt->total, sweep, st);
+    if (e != cudaSuccess) return cs::set_error(CS_ERR_CUDA, cudaGetErrorString(e));
+    return CS_OK;
+}
+
+}  // namespace cs
+
+extern "C" {
+
+CS_API cs_status cs_batch_create(cs_batch **out, cs_plan *const *plans, void *const *a, void *const *b,
+                                 int count)
+{
+    return cs::batch_create_ex(out, plans, a, b, count, nullptr, true, nullptr);
 }
 
 CS_API cs_status cs_batch_run(cs_batch *bt, long long steps, void *stream, int *result_in_b)
@@ -534,9 +579,9 @@ CS_API cs_status cs_batch_run(cs_batch *bt, long long steps, void *stream, int *
                 bt->tc ? cs::launch_tc_batch(!bt->split, bt->d_items[par], bt->count, bt->total, bt->wait, st)
                 : bt->dims == 2
                     ? dispatch(bt->radius, bt->pattern, bt->split, (const Item *)bt->d_items[par], bt->count,
-                               bt->d_w, bt->total, st)
+                               bt->d_w, bt->total, 0, st)
                     : dispatch3(bt->radius, bt->pattern, bt->split, (const Item3 *)bt->d_items[par], bt->count,
-                                bt->d_w, bt->total, st);
+                                bt->d_w, bt->total, 0, st);
             if (e != cudaSuccess) return e;
             par ^= 1;
         }
@@ -576,8 +621,8 @@ CS_API cs_status cs_batch_destroy(cs_batch *bt)
     if (!bt) return CS_OK;
     for (auto &kv : bt->graphs) cudaGraphExecDestroy(kv.second);
     for (void *p : bt->d_items)
-        if (p) cudaFree(p);
-    if (bt->d_w) cudaFree(bt->d_w);
+        if (p) bt->stream_mem ? cudaFreeAsync(p, bt->mem_stream) : cudaFree(p);
+    if (bt->d_w) bt->stream_mem ? cudaFreeAsync(bt->d_w, bt->mem_stream) : cudaFree(bt->d_w);
     delete bt;
     return CS_OK;
 }

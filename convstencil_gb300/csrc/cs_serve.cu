@@ -23,6 +23,7 @@
 // and in any mix.
 #include "../../include/convstencil.h"
 #include "cs_internal.h"
+#include "cs_plan_internal.h"
 
 #include <algorithm>
 #include <atomic>
@@ -36,11 +37,6 @@
 #include <string>
 #include <thread>
 #include <vector>
-
-namespace cs {
-cs_status run_from(cs_plan *p, void *a, void *b, long long first_sweep, long long steps, cudaStream_t st,
-                   int *result_in_b);
-}  // namespace cs
 
 namespace {
 
