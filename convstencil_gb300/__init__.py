@@ -122,7 +122,7 @@ class ServerStats(ctypes.Structure):
                 ("hbm_budget_bytes", ctypes.c_longlong), ("hbm_reserved_bytes", ctypes.c_longlong),
                 ("p50_s", ctypes.c_double), ("p99_s", ctypes.c_double), ("mean_s", ctypes.c_double),
                 ("point_steps", ctypes.c_double), ("wall_s", ctypes.c_double),
-                ("gstencil_s", ctypes.c_double)]
+                ("gstencil_s", ctypes.c_double), ("packed", ctypes.c_longlong)]
 
 
 _lib = None
@@ -178,6 +178,7 @@ def lib() -> ctypes.CDLL:
     L.cs_batch_destroy.argtypes = [vp]
     L.cs_server_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]
     L.cs_server_submit.argtypes = [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ll)]
+    L.cs_server_submit_many.argtypes = [vp, ctypes.POINTER(RequestDesc), i, ctypes.POINTER(ll)]
     L.cs_server_wait.argtypes = [vp, ll, dp, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
     L.cs_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
     L.cs_server_destroy.argtypes = [vp]
@@ -433,6 +434,31 @@ class Server:
         check(lib().cs_server_submit(self._h, ctypes.byref(d), ctypes.byref(rid)))
         self._shapes[int(rid.value)] = x.shape
         return int(rid.value)
+
+    def submit_many(self, requests) -> list:
+        """Submits (shape, interior, weights, steps[, precision[, semantics]])
+        tuples at once; small requests of one family among them run as one
+        batch. Returns their ids."""
+        descs, keep = [], []
+        for req in requests:
+            shape, interior, weights, steps = req[:4]
+            precision = req[4] if len(req) > 4 else Precision.FP64
+            semantics = req[5] if len(req) > 5 else Semantics.STEP
+            if isinstance(shape, str):
+                shape = SHAPE_BY_NAME[shape]
+            x = np.ascontiguousarray(interior, np.float64)
+            w = np.ascontiguousarray(np.asarray(weights, np.float64).reshape(-1))
+            keep += [x, w]
+            ext = list(x.shape) + [1] * (3 - x.ndim)
+            descs.append(RequestDesc(int(shape), int(semantics), int(precision), (ctypes.c_longlong * 3)(*ext),
+                                     _dptr(w), int(w.size), _dptr(x), int(steps)))
+        n = len(descs)
+        arr = (RequestDesc * n)(*descs)
+        ids = (ctypes.c_longlong * n)()
+        check(lib().cs_server_submit_many(self._h, arr, n, ids))
+        for req, rid in zip(requests, ids):
+            self._shapes[int(rid)] = np.asarray(req[1]).shape
+        return [int(v) for v in ids]
 
     def wait(self, rid: int, timeout: float = 0.0):
         out = np.empty(self._shapes.pop(rid), np.float64)

@@ -1247,6 +1247,7 @@ bool plan_facts(const cs_plan *p, PlanFacts *f)
     f->origin = p->layout.origin;
     f->elements = p->layout.elements;
     f->reanchor = p->reanchor;
+    f->algo = p->algo;
     f->w = &p->w;
     return true;
 }

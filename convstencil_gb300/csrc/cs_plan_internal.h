@@ -15,6 +15,7 @@ struct PlanFacts {
     GridView view;
     long long origin, elements;
     long long reanchor;  // split: FP64 re-anchor interval in sweeps (0 = never)
+    int algo;            // the pinned cs_algo (CS_ALGO_AUTO: the tuner's)
     const Weights *w;
 };
 bool plan_facts(const cs_plan *p, PlanFacts *f);

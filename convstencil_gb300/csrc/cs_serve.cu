@@ -11,6 +11,13 @@
 //     CUDA graph and replayed. Small requests (a few ms of work or less) are
 //     issued whole, chunk after chunk, on high-priority streams, so the
 //     hardware runs their kernels ahead of the large requests' chunks;
+//   * packing: small requests of one family (dims, radius, tap pattern,
+//     precision, steps per sweep) admitted in the same turn run together as
+//     one batch (cs_batch_*), one launch per sweep for all of them, each
+//     grid leaving the batch after its own sweep count; the batch kernels do
+//     each point's arithmetic as the request's own kernel would, and FP64
+//     re-anchor sweeps fall at the same sweep counts, so a packed result is
+//     the one the request gets alone;
 //   * completion: the result goes to a pinned host buffer, the device memory is
 //     released (making room for queued requests), the latency is recorded. A
 //     request during whose life a bounded device-side wait expired (the
@@ -36,6 +43,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 namespace {
@@ -107,6 +115,8 @@ struct Request {
     cudaEvent_t chunk_ev = nullptr, done_ev = nullptr;
     bool chunk_pending = false;
     bool small = false;     // little work: issued whole, on a high-priority stream
+    bool packable = false;  // small, on a kernel the batcher runs with the same arithmetic
+    bool packed = false;    // ran in a batch with other requests of its family
     cudaGraphExec_t graph = nullptr;
     long long graph_steps = 0;
     int full_chunks = 0;
@@ -141,6 +151,7 @@ struct cs_server {
     double point_steps = 0, t_first = 0, t_last = 0;
     int rr = 0, rr_fast = 0;
     int sm_count = 1;
+    long long packed = 0;  // requests that ran in shared batch launches
 };
 
 namespace {
@@ -292,6 +303,70 @@ void advance(cs_server *s, Request *r)
     }
 }
 
+// Runs a family of admitted small requests (two or more) as one batch on a
+// high-priority stream: after their uploads, one launch per sweep for every
+// member still running (members with fewer sweeps leave the batch), an FP64
+// re-anchor sweep per split member wherever it would take one alone, and each
+// member's result copied out right after its last sweep. Returns false (and
+// leaves the members to the normal path) if the batch cannot be set up.
+bool run_pack(cs_server *s, std::vector<Request *> &grp)
+{
+    const int n = (int)grp.size();
+    cudaStream_t st = s->fast_streams[s->rr_fast++ % s->fast_streams.size()];
+    std::vector<cs_plan *> plans(n);
+    std::vector<void *> a(n), b(n);
+    std::vector<long long> sweeps(n);
+    long long most = 0;
+    for (int i = 0; i < n; ++i) {
+        Request *r = grp[i];
+        // the member's upload (on its own stream) comes first
+        if (cudaEventRecord(r->chunk_ev, r->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(st, r->chunk_ev, 0) != cudaSuccess)
+            return false;
+        plans[i] = r->plan;
+        a[i] = r->d[0];
+        b[i] = r->d[1];
+        sweeps[i] = r->steps / r->sweeps_per_step;
+        most = std::max(most, sweeps[i]);
+    }
+    cs_batch *bt = nullptr;
+    if (cs::batch_create_ex(&bt, plans.data(), a.data(), b.data(), n, sweeps.data(), false, st) != CS_OK)
+        return false;
+    cs::PlanFacts f;
+    cs::plan_facts(grp[0]->plan, &f);
+    for (Request *r : grp) {
+        r->stream = st;  // every later operation of the member is ordered on the batch's stream
+        r->packed = true;
+    }
+    cs_status err = CS_OK;
+    for (long long j = 0; j < most && err == CS_OK; ++j) {
+        const bool anchor = f.prec == CS_PREC_SPLIT && f.reanchor > 0 && (j + 1) % f.reanchor == 0;
+        if (anchor) {
+            for (int i = 0; i < n && err == CS_OK; ++i)
+                if (sweeps[i] > j && cs::fp64_anchor_sweep(grp[i]->plan, grp[i]->d[j & 1], grp[i]->d[(j & 1) ^ 1],
+                                                          st) != cudaSuccess)
+                    err = CS_ERR_CUDA;
+        } else {
+            err = cs::batch_sweep(bt, j, st);
+        }
+        for (int i = 0; i < n && err == CS_OK; ++i)
+            if (sweeps[i] == j + 1) {
+                grp[i]->cur = (int)((j + 1) & 1);
+                grp[i]->issued = grp[i]->steps;
+                finish_request(grp[i]);
+            }
+    }
+    cs_batch_destroy(bt);  // tables freed in order on st
+    for (Request *r : grp)
+        if (r->state == State::Active) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            fail_request(s, r, err == CS_OK ? CS_ERR_CUDA : err, "batched sweep launch failed");
+        }
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->packed += n;
+    return true;
+}
+
 void worker_main(cs_server *s)
 {
     cudaSetDevice(s->device);
@@ -320,6 +395,7 @@ void worker_main(cs_server *s)
                 admitted.push_back(r);
             }
         }
+        std::map<std::tuple<int, int, int, int, int>, std::vector<Request *>> families;
         for (Request *r : admitted) {
             if (!start_request(s, r)) {
                 std::lock_guard<std::mutex> lk(s->mu);
@@ -328,8 +404,14 @@ void worker_main(cs_server *s)
                 s->active.erase(std::find(s->active.begin(), s->active.end(), r));
                 r->retired = true;
                 s->cv_done.notify_all();
+            } else if (r->packable) {
+                cs::PlanFacts f;
+                cs::plan_facts(r->plan, &f);
+                families[std::make_tuple(f.dims, f.radius, f.pattern, (int)f.prec, f.steps_per_sweep)].push_back(r);
             }
         }
+        for (auto &kv : families)
+            if (kv.second.size() >= 2) run_pack(s, kv.second);
         std::vector<Request *> act;
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -443,9 +525,15 @@ CS_API cs_status cs_server_create(cs_server **out, const cs_server_config *cfg)
     return CS_OK;
 }
 
-CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long long *id)
+}  // extern "C"
+
+namespace {
+
+// Everything a request needs before it is queued: plan, kernel choice,
+// packed host copy of its input (no server lock held).
+cs_status prepare_request(cs_server *s, const cs_request_desc *d, std::unique_ptr<Request> &out)
 {
-    if (!s || !d || !id || !d->interior_in || !d->weights || d->steps < 0) return CS_ERR_INVALID_ARGUMENT;
+    if (!d || !d->interior_in || !d->weights || d->steps < 0) return CS_ERR_INVALID_ARGUMENT;
     auto r = std::make_unique<Request>();
     cs_status st = cs_plan_create(&r->plan, d->shape, d->semantics, d->precision, d->extent, d->weights,
                                   d->n_weights, nullptr);
@@ -491,6 +579,12 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
               cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_TC) == CS_OK))
             cs_plan_set_option(r->plan, CS_OPT_ALGO, CS_ALGO_FP64_FMA);
     }
+    // The FP64 FMA 2D kernel's tile rows: fixed here (the plan tuner would
+    // time both on the worker thread); results do not depend on them.
+    if (d->precision == CS_PREC_FP64 && (d->shape >= CS_SHAPE_STAR2D1R && d->shape <= CS_SHAPE_BOX2D3R)) {
+        const long long t32 = ((d->extent[1] + 63) / 64) * ((d->extent[0] + 31) / 32);
+        cs_plan_set_option(r->plan, CS_OPT_TILE_ROWS, t32 < 6LL * s->sm_count ? 16 : 32);
+    }
     long long sweeps1 = 0;
     if (d->semantics == CS_SEM_FUSED) {
         for (long long k = 1; k <= 3; ++k)
@@ -517,6 +611,16 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
         const double work = pts * (double)sweeps1 * taps / (d->precision == CS_PREC_SPLIT ? 8.0 : 1.0);
         r->small = work < kSmallWork;
     }
+    {
+        // Packable: small, 2D (not radius 3: those run tcgen05 or mma.sync
+        // kernels alone) or 3D, on the FP64 FMA or double-float kernels whose
+        // per-point arithmetic the batch kernels repeat.
+        cs::PlanFacts f;
+        cs::plan_facts(r->plan, &f);
+        const int fma = d->precision == CS_PREC_SPLIT ? CS_ALGO_SPLIT_FMA : CS_ALGO_FP64_FMA;
+        r->packable = r->small && f.algo == fma &&
+                      ((f.dims == 2 && f.radius != 3) || (f.dims == 3 && (f.radius == 1 || f.radius == 3)));
+    }
     r->bytes = r->layout.bytes * (d->precision == CS_PREC_SPLIT ? 3 : 2);
     r->host = s->pinned.get(r->layout.bytes, &r->host_cls);
     if (!r->host) {
@@ -524,13 +628,19 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
         return CS_ERR_OUT_OF_MEMORY;
     }
     pack(r->layout, d->interior_in, (double *)r->host);
-    std::lock_guard<std::mutex> lk(s->mu);
+    out = std::move(r);
+    return CS_OK;
+}
+
+// Queues a prepared request (server lock held).
+long long enqueue(cs_server *s, std::unique_ptr<Request> r)
+{
     r->id = s->next_id++;
     r->t_submit = now_s();
     if (s->t_first == 0) s->t_first = r->t_submit;
-    *id = r->id;
+    const long long id = r->id;
     Request *raw = r.get();
-    s->all[r->id] = std::move(r);
+    s->all[id] = std::move(r);
     if (raw->steps == 0) {  // nothing to run: the result is the input
         raw->state = State::Done;
         raw->retired = true;
@@ -540,8 +650,48 @@ CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long l
         s->cv_done.notify_all();
     } else {
         s->queue.push_back(raw);
-        s->cv_work.notify_one();
     }
+    return id;
+}
+
+void discard(cs_server *s, std::unique_ptr<Request> &r)
+{
+    if (!r) return;
+    if (r->host) s->pinned.put(r->host, r->host_cls);
+    cs_plan_destroy(r->plan);
+    r.reset();
+}
+
+}  // namespace
+
+extern "C" {
+
+CS_API cs_status cs_server_submit(cs_server *s, const cs_request_desc *d, long long *id)
+{
+    if (!s || !id) return CS_ERR_INVALID_ARGUMENT;
+    std::unique_ptr<Request> r;
+    const cs_status st = prepare_request(s, d, r);
+    if (st != CS_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *id = enqueue(s, std::move(r));
+    s->cv_work.notify_one();
+    return CS_OK;
+}
+
+CS_API cs_status cs_server_submit_many(cs_server *s, const cs_request_desc *reqs, int count, long long *ids)
+{
+    if (!s || !reqs || !ids || count < 1) return CS_ERR_INVALID_ARGUMENT;
+    std::vector<std::unique_ptr<Request>> rs(count);
+    for (int i = 0; i < count; ++i) {
+        const cs_status st = prepare_request(s, &reqs[i], rs[i]);
+        if (st != CS_OK) {
+            for (auto &r : rs) discard(s, r);
+            return st;
+        }
+    }
+    std::lock_guard<std::mutex> lk(s->mu);  // one lock: the worker sees all of them at once
+    for (int i = 0; i < count; ++i) ids[i] = enqueue(s, std::move(rs[i]));
+    s->cv_work.notify_one();
     return CS_OK;
 }
 
@@ -594,6 +744,7 @@ CS_API cs_status cs_server_get_stats(cs_server *s, cs_server_stats *out)
     out->point_steps = s->point_steps;
     out->wall_s = s->t_last > s->t_first ? s->t_last - s->t_first : 0.0;
     out->gstencil_s = out->wall_s > 0 ? s->point_steps / out->wall_s / 1e9 : 0.0;
+    out->packed = s->packed;
     return CS_OK;
 }
 

@@ -259,7 +259,9 @@ CS_API cs_status cs_batch_destroy(cs_batch *batch);
  * budget and a slot is free, keeps their grids device-resident, and issues
  * one chunk of sweeps per active request per turn on a pool of streams (the
  * work of different requests overlaps on the GPU; full chunks are replayed as
- * captured CUDA graphs). Kernel choice and re-anchoring depend only on the
+ * captured CUDA graphs). Small requests of one family (2D radius 1-2 or 3D,
+ * same radius, tap pattern, precision) admitted in the same turn share batch
+ * launches. Kernel choice and re-anchoring depend only on the
  * request, so a result is bitwise the same alone and in any mix. Not in the
  * reference (its CLIs run one solve per process). */
 typedef struct cs_server cs_server;
@@ -287,12 +289,19 @@ typedef struct cs_server_stats {
     double point_steps;          /* interior points x steps of completed requests */
     double wall_s;               /* first submit -> last completion */
     double gstencil_s;           /* point_steps / wall_s / 1e9 */
+    long long packed;            /* requests that ran in shared batch launches */
 } cs_server_stats;
 
 /* cfg NULL = defaults. Uses the calling thread's current device. */
 CS_API cs_status cs_server_create(cs_server **server, const cs_server_config *cfg);
 /* Copies the input; returns at once with the request id. */
 CS_API cs_status cs_server_submit(cs_server *server, const cs_request_desc *req, long long *id);
+/* Submits `count` requests at once (ids[i] for reqs[i]); the worker sees them
+ * together, so small requests of one family among them are admitted in the
+ * same turn and run as one batch (one launch per sweep for all of them).
+ * On an invalid request nothing is submitted. */
+CS_API cs_status cs_server_submit_many(cs_server *server, const cs_request_desc *reqs, int count,
+                                       long long *ids);
 /* Waits (timeout_seconds <= 0: no limit) and copies the dense interior result
  * to interior_out (may be NULL). Returns the request's status (e.g.
  * CS_ERR_OUT_OF_MEMORY if it can never fit the budget), CS_ERR_TIMEOUT if not

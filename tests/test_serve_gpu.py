@@ -118,3 +118,33 @@ def test_zero_steps_and_fused_requests():
     p = cs.Plan("box2d1r", x.shape, w49, semantics=cs.Semantics.FUSED)
     ref = p.unpack(p.run_host(p.pack(x), 9))
     assert rel_err(got, ref)[0] <= 1e-12
+
+
+def test_small_requests_of_one_family_share_batch_launches():
+    """Small requests submitted together run as batches per family (2D
+    radius 1, 3D star and box, FP64 and split), each grid leaving its batch
+    after its own step count; every result equals the request served alone
+    (value-equal, -0.0 == 0.0) and the oracle, split runs past 100 steps
+    take their FP64 re-anchor sweeps inside the batch."""
+    rng = np.random.default_rng(11)
+    reqs = []
+    for i, (shape, prec) in enumerate([(s, p) for s in ("star2d1r", "box2d1r", "star3d1r", "box3d1r")
+                                       for p in (cs.Precision.FP64, cs.Precision.SPLIT)] * 3):
+        info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
+        ext = tuple(int(v) for v in (rng.integers(20, 120, 2) if info[0] == 2 else rng.integers(8, 30, 3)))
+        steps = int(rng.integers(5, 220))
+        w = O.seeded_weights(info[1], 300 + i)
+        x = O.splitmix_uniform(int(np.prod(ext)), 400 + i).reshape(ext)
+        reqs.append((shape, x, w, steps, prec))
+    with cs.Server(streams=4, max_active=64, chunk_steps=16) as srv:
+        ids = srv.submit_many(reqs)
+        packed = [srv.wait(i, timeout=120)[0] for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["packed"] >= len(reqs) // 2, st
+    for req, got in zip(reqs, packed):
+        with cs.Server(streams=1, max_active=1) as alone:
+            ref_alone = alone.wait(alone.submit(*req[:4], precision=req[4]), timeout=120)[0]
+        np.testing.assert_array_equal(got, ref_alone)
+        tol = 1e-12 if req[4] == cs.Precision.FP64 else 1e-10
+        assert rel_err(got, _oracle(req[0], req[1], req[2], req[3]))[0] <= tol, req[:1] + req[3:]
