@@ -11,8 +11,8 @@
 //     CUDA graph and replayed. Small requests (a few ms of work or less) are
 //     issued whole, chunk after chunk, on high-priority streams, so the
 //     hardware runs their kernels ahead of the large requests' chunks;
-//   * packing: small requests of one family (dims, radius, tap pattern,
-//     precision, steps per sweep) admitted in the same turn run together as
+//   * packing: small FP64 requests of one family (dims, radius, tap pattern,
+//     steps per sweep; 2D radius 1-2 and 3D) admitted in the same turn run together as
 //     one batch (cs_batch_*), one launch per sweep for all of them, each
 //     grid leaving the batch after its own sweep count; the batch kernels do
 //     each point's arithmetic as the request's own kernel would, and FP64
@@ -612,13 +612,17 @@ cs_status prepare_request(cs_server *s, const cs_request_desc *d, std::unique_pt
         r->small = work < kSmallWork;
     }
     {
-        // Packable: small, 2D (not radius 3: those run tcgen05 or mma.sync
-        // kernels alone) or 3D, on the FP64 FMA or double-float kernels whose
-        // per-point arithmetic the batch kernels repeat.
+        // Packable: small FP64 requests, 2D (not radius 3: those run tcgen05
+        // alone from four tiles per SM) or 3D, on the FP64 FMA kernels whose
+        // per-point arithmetic and form the batch kernels repeat. Split
+        // requests stay alone: their own kernels (temporal blocking in 2D, the
+        // z-queue star and packed-pair box in 3D) beat the batch's generic
+        // double-float form (measured, 48 saturated split requests: 104
+        // GStencil/s alone, 85 with all small split requests packed, 90 with
+        // the 3D ones packed; FP64 31.3 alone, 31.0 packed).
         cs::PlanFacts f;
         cs::plan_facts(r->plan, &f);
-        const int fma = d->precision == CS_PREC_SPLIT ? CS_ALGO_SPLIT_FMA : CS_ALGO_FP64_FMA;
-        r->packable = r->small && f.algo == fma &&
+        r->packable = r->small && d->precision == CS_PREC_FP64 && f.algo == CS_ALGO_FP64_FMA &&
                       ((f.dims == 2 && f.radius != 3) || (f.dims == 3 && (f.radius == 1 || f.radius == 3)));
     }
     r->bytes = r->layout.bytes * (d->precision == CS_PREC_SPLIT ? 3 : 2);

@@ -259,8 +259,8 @@ CS_API cs_status cs_batch_destroy(cs_batch *batch);
  * budget and a slot is free, keeps their grids device-resident, and issues
  * one chunk of sweeps per active request per turn on a pool of streams (the
  * work of different requests overlaps on the GPU; full chunks are replayed as
- * captured CUDA graphs). Small requests of one family (2D radius 1-2 or 3D,
- * same radius, tap pattern, precision) admitted in the same turn share batch
+ * captured CUDA graphs). Small FP64 requests of one family (2D radius 1-2
+ * or 3D, same radius and tap pattern) admitted in the same turn share batch
  * launches. Kernel choice and re-anchoring depend only on the
  * request, so a result is bitwise the same alone and in any mix. Not in the
  * reference (its CLIs run one solve per process). */
