@@ -25,6 +25,7 @@
 #include <new>
 #include <string>
 #include <tuple>
+#include <vector>
 
 namespace cs {
 
@@ -286,19 +287,26 @@ bool split_tc3d_ok(const cs_plan *p)
     return p->prec == CS_PREC_SPLIT && p->dims == 3 && p->radius == 1;
 }
 
-cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *out_base,
-                         cudaStream_t st)
+// One sweep over the slabs [row0, row0 + rows) of the slowest axis (rows of
+// a 2D grid, planes of a 3D one). The slabs on either side are read as the
+// grid's own data, so a sweep may be split into bands this way; the
+// temporally blocked kernels, which treat everything outside their grid as
+// zero, are never launched here.
+cudaError_t launch_sweep_rows(const cs_plan *p, int algo, const void *in_base, void *out_base, long long row0,
+                              long long rows, cudaStream_t st)
 {
-    const long long off = p->layout.origin;
+    GridView v = p->view;
+    v.ext[0] = rows;
+    const long long off = p->layout.origin + row0 * p->view.pitch[0];
     if (p->prec == CS_PREC_FP64) {
         const double *in = (const double *)in_base + off;
         double *out = (double *)out_base + off;
-        if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(p->view, p->w, in, out, st);
+        if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(v, p->w, in, out, st);
         if (algo == CS_ALGO_FP64_TC && fp64_tc_ok(p) && reinterpret_cast<uintptr_t>(out_base) % 16 == 0 &&
-            cs::split_tma_layout_ok(p->view, off, in_base))
-            return cs::launch_fp64_sweep_tc(p->view, p->w, off, p->layout.elements, (const double *)in_base,
+            cs::split_tma_layout_ok(v, off, in_base))
+            return cs::launch_fp64_sweep_tc(v, p->w, off, p->layout.elements, (const double *)in_base,
                                             (double *)out_base, p->wait, st);
-        return cs::launch_fp64_fma(p->view, p->radius, p->pattern, p->w, in, out, st, p->active_rows);
+        return cs::launch_fp64_fma(v, p->radius, p->pattern, p->w, in, out, st, p->active_rows);
     }
     // The tensor-core split kernels store float4 (two points) at even element
     // offsets, so they need a 16-byte aligned output base; the TMA-fed ones
@@ -307,25 +315,30 @@ cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *
     const bool out16 = (reinterpret_cast<uintptr_t>(out_base) % 16) == 0;
     if (p->dims == 3) {
         if (algo == CS_ALGO_SPLIT_TC && split_tc3d_ok(p) &&
-            cs::split_tc3d_layout_ok(p->view, off, in_base, out_base))
-            return cs::launch_split_sweep_tc3d(p->view, p->w, off, p->layout.elements,
+            cs::split_tc3d_layout_ok(v, off, in_base, out_base))
+            return cs::launch_split_sweep_tc3d(v, p->w, off, p->layout.elements,
                                                (const float2 *)in_base, (float2 *)out_base, p->wait, st);
         algo = CS_ALGO_SPLIT_FMA;
     }
-    const bool tma_ok = out16 && cs::split_tma_layout_ok(p->view, off, in_base);
+    const bool tma_ok = out16 && cs::split_tma_layout_ok(v, off, in_base);
     if (algo == CS_ALGO_SPLIT_TC && tma_ok)
-        return cs::launch_split_sweep_tc(p->view, p->w, off, p->layout.elements,
+        return cs::launch_split_sweep_tc(v, p->w, off, p->layout.elements,
                                          (const float2 *)in_base, (float2 *)out_base, p->wait, st);
     if (algo == CS_ALGO_SPLIT_MMA_TMA && tma_ok)
-        return cs::launch_split_sweep_tma(p->view, p->w, off, p->layout.elements,
+        return cs::launch_split_sweep_tma(v, p->w, off, p->layout.elements,
                                           (const float2 *)in_base, (float2 *)out_base, st);
     if (algo == CS_ALGO_SPLIT_MMA_TMA || algo == CS_ALGO_SPLIT_TC)
         algo = CS_ALGO_SPLIT_MMA;  // buffer not TMA-aligned
     if (algo == CS_ALGO_SPLIT_MMA && !out16) algo = CS_ALGO_SPLIT_FMA;
     const float2 *in = (const float2 *)in_base + off;
     float2 *out = (float2 *)out_base + off;
-    return cs::launch_split_sweep(p->view, p->radius, p->pattern, p->w, algo == CS_ALGO_SPLIT_MMA,
+    return cs::launch_split_sweep(v, p->radius, p->pattern, p->w, algo == CS_ALGO_SPLIT_MMA,
                                   in, out, st);
+}
+
+cudaError_t launch_sweep(const cs_plan *p, int algo, const void *in_base, void *out_base, cudaStream_t st)
+{
+    return launch_sweep_rows(p, algo, in_base, out_base, 0, p->view.ext[0], st);
 }
 
 int size_class(const cs_plan *p)
@@ -344,7 +357,7 @@ int size_class(const cs_plan *p)
 // candidate, the first sweep of the first run is timed once per candidate
 // (every candidate computes the same sweep a -> b, so the extra work changes
 // no result) and the winner is remembered for plans of the same class.
-cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *out)
+cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *out, bool may_time = true)
 {
     int cand[4];
     int nc = 0;
@@ -387,6 +400,10 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
             *out = it->second;
             return CS_OK;
         }
+    }
+    if (!may_time) {  // the caller cannot afford a timing run now
+        *out = -1;
+        return CS_OK;
     }
     float best_ms = 1e30f;
     int best = cand[0];
@@ -923,6 +940,97 @@ struct DevBuf {
 
 // in_elems doubles from host_in into buffer 0 (buffer 1 zero), `sweeps`
 // sweeps, then out_elems doubles from result + out_offset to host_out.
+// Host-buffer run with the copies overlapped: the grid goes to the device in
+// row bands (slabs of the slowest axis) on one stream while the sweeps run
+// as a wavefront over the bands on another (sweep s of band k once sweep
+// s - 1 of bands k - 1 .. k + 1 is done, band k + 1 of the input having
+// arrived for the first sweep), and each band goes back as soon as its last
+// sweep is done. Launches are issued diagonal by diagonal on one stream, so
+// sweep s of band k always precedes sweep s + 1 of band k - 1, which
+// overwrites rows that it reads. Used when the kernel is known without a
+// timing run, no temporal blocking and no re-anchor sweep is involved, and
+// the whole grid goes both ways.
+bool banded_ok(cs_plan *p, long long sweeps, int *algo, int *bands)
+{
+    if (p->dims < 2 || sweeps < 1) return false;
+    if (p->prec == CS_PREC_SPLIT && cs::split_tb_supported(p->dims, p->radius, p->pattern) && p->time_block != 1)
+        return false;
+    if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && sweeps >= p->reanchor) return false;
+    if (choose_algo(p, nullptr, nullptr, nullptr, algo, false) != CS_OK || *algo < 0) return false;
+    const long long slabs = p->view.ext[0];
+    const long long per = p->dims == 2 ? 1024 : 64;  // slabs per band at least
+    *bands = (int)std::min<long long>(8, slabs / per);
+    return *bands >= 2;
+}
+
+cs_status host_run_banded(cs_plan *p, int algo, int bands, const double *host_in, double *host_out,
+                          long long sweeps, void *const d[2], double *loop_seconds)
+{
+    const long long ld0 = p->view.pitch[0];        // elements per slab
+    const long long total = p->layout.elements / ld0;  // slabs in the buffer, halo included
+    const long long first = p->layout.origin / ld0;    // halo slabs before the interior
+    const long long slabs = p->view.ext[0];
+    const long long align = p->dims == 2 ? 64 : 8;
+    std::vector<long long> b(bands + 1);  // interior slab boundaries of the bands
+    for (int k = 0; k <= bands; ++k) b[k] = std::min(slabs, (slabs * k / bands + align - 1) / align * align);
+    b[bands] = slabs;
+    std::vector<long long> c(bands + 1);  // buffer slab boundaries of the copy chunks
+    for (int k = 0; k <= bands; ++k) c[k] = k == 0 ? 0 : k == bands ? total : first + b[k];
+    struct Streams {
+        cudaStream_t s[3] = {nullptr, nullptr, nullptr};
+        std::vector<cudaEvent_t> ev;
+        ~Streams()
+        {
+            for (cudaEvent_t e : ev) cudaEventDestroy(e);
+            for (cudaStream_t x : s)
+                if (x) cudaStreamDestroy(x);
+        }
+    } S;
+    for (auto &x : S.s) CS_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    cudaStream_t sc = S.s[0], sh = S.s[1], sd = S.s[2];
+    S.ev.resize(2 * bands + 2);
+    for (auto &e : S.ev) CS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDefault));
+    cudaEvent_t *in_ev = S.ev.data(), *out_ev = S.ev.data() + bands, e0 = S.ev[2 * bands], e1 = S.ev[2 * bands + 1];
+    const size_t slab_bytes = (size_t)ld0 * sizeof(double);
+    CS_CUDA(cudaMemsetAsync(d[1], 0, (size_t)p->layout.bytes, sc));  // the second grid's halo reads as zero
+    for (int k = 0; k < bands; ++k) {
+        const long long cnt = (c[k + 1] - c[k]) * ld0;
+        char *dst = (char *)d[0] + c[k] * slab_bytes;
+        CS_CUDA(cudaMemcpyAsync(dst, host_in + c[k] * ld0, (size_t)cnt * sizeof(double), cudaMemcpyHostToDevice, sh));
+        if (p->prec == CS_PREC_SPLIT) CS_CUDA(cs::launch_fp64_to_split_inplace(cnt, dst, sh));
+        CS_CUDA(cudaEventRecord(in_ev[k], sh));
+    }
+    CS_CUDA(cudaEventRecord(e0, sc));
+    void *f = d[sweeps & 1];  // final grid
+    for (long long diag = 0; diag < bands + sweeps - 1; ++diag) {
+        for (long long sw = std::max(0LL, diag - (bands - 1)); sw <= std::min(sweeps - 1, diag); ++sw) {
+            const int k = (int)(diag - sw);
+            if (sw == 0) {
+                CS_CUDA(cudaStreamWaitEvent(sc, in_ev[k], 0));
+                if (k + 1 < bands) CS_CUDA(cudaStreamWaitEvent(sc, in_ev[k + 1], 0));
+            }
+            CS_CUDA(launch_sweep_rows(p, algo, d[sw & 1], d[(sw + 1) & 1], b[k], b[k + 1] - b[k], sc));
+            if (sw == sweeps - 1) {  // band k is final: back to the host now
+                const long long cnt = (c[k + 1] - c[k]) * ld0;
+                char *src = (char *)f + c[k] * slab_bytes;
+                if (p->prec == CS_PREC_SPLIT) CS_CUDA(cs::launch_split_to_fp64_inplace(cnt, src, sc));
+                CS_CUDA(cudaEventRecord(out_ev[k], sc));
+                CS_CUDA(cudaStreamWaitEvent(sd, out_ev[k], 0));
+                CS_CUDA(cudaMemcpyAsync(host_out + c[k] * ld0, src, (size_t)cnt * sizeof(double),
+                                        cudaMemcpyDeviceToHost, sd));
+            }
+        }
+    }
+    CS_CUDA(cudaEventRecord(e1, sc));
+    CS_CUDA(cudaStreamSynchronize(sd));
+    CS_CUDA(cudaStreamSynchronize(sc));
+    float ms = 0.f;
+    CS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (loop_seconds) *loop_seconds = ms * 1e-3;
+    t_loop_seconds = ms * 1e-3;
+    return CS_OK;
+}
+
 cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *host_out,
                    size_t out_offset, size_t out_elems, long long steps, double *loop_seconds)
 {
@@ -953,10 +1061,26 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
         d[0] = own[0].p;
         d[1] = own[1].p;
     }
+    const bool whole = in_elems * elem_bytes == bytes;
+    int balgo = 0, bands = 0;
+    if (whole && out_offset == 0 && out_elems == (size_t)n && banded_ok(p, sweeps, &balgo, &bands)) {
+        unsigned w0 = 0, w1 = 0;
+        s = cs_device_wait_timeouts(&w0, 0);
+        if (s != CS_OK) return s;
+        s = host_run_banded(p, balgo, bands, host_in, host_out, sweeps, d, loop_seconds);
+        if (s != CS_OK) return s;
+        p->last_algo = balgo;
+        p->last_time_block = 1;
+        s = cs_device_wait_timeouts(&w1, 0);
+        if (s != CS_OK) return s;
+        if (w1 != w0)
+            return fail(CS_ERR_TIMEOUT, "%u bounded device-side wait(s) expired during the run; the result is incomplete",
+                        w1 - w0);
+        return CS_OK;
+    }
     // The copy fills the first grid completely unless the caller passes a
     // part of it; the second grid's halo must read as zero. A split plan's
     // grid is converted from FP64 in place (same 8 bytes per point).
-    const bool whole = in_elems * elem_bytes == bytes;
     if (!whole) CS_CUDA(cudaMemset(d[0], 0, bytes));
     CS_CUDA(cudaMemset(d[1], 0, bytes));
     CS_CUDA(cudaMemcpy(d[0], host_in, in_elems * elem_bytes, cudaMemcpyHostToDevice));
