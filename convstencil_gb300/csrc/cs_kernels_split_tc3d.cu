@@ -64,12 +64,12 @@ using split::two_sum;
 using namespace tc;
 
 // Warp roles.
-constexpr int kSliceWarps = 8, kEpiWarps = 8;
+constexpr int kGroups = 3, kGroupWarps = 4;  // slicer groups of four warps take every third plane
+constexpr int kSliceWarps = kGroups * kGroupWarps, kEpiWarps = 8;
 constexpr int kWarpTma = 0, kWarpMma = 1, kWarpSlice0 = 2, kWarpEpi0 = kWarpSlice0 + kSliceWarps;
-constexpr int kThreads = 32 * (kWarpEpi0 + kEpiWarps);  // 576
-constexpr int kGroupWarps = kSliceWarps / 2;  // two slicer groups take alternate planes
+constexpr int kThreads = 32 * (kWarpEpi0 + kEpiWarps);  // 704
 constexpr int kGroupThreads = 32 * kGroupWarps;
-constexpr int kSliceBarrier = 1;             // named barriers 1 and 2: one per slicer group
+constexpr int kSliceBarrier = 1;             // named barriers 1 .. kGroups: one per slicer group
 
 constexpr int G = 16;                        // output rows per tile (M = G x 8 blocks = 128)
 constexpr int TX = 64, TY = G;               // output tile 16 x 64
@@ -81,12 +81,17 @@ constexpr int NLV = 32;                      // TMEM columns per level: 4 tap pl
 constexpr int NCOL = NLV * kDigits;          // 160 columns per input-plane block
 constexpr int NBLK = 3;                      // input-plane blocks in TMEM (ring)
 constexpr int kTmemCols = 512;
-constexpr int kStages = 4;                   // TMA window buffers (two per slicer group)
+constexpr int kStages = 2 * kGroups;         // TMA window buffers (two per slicer group)
 constexpr int NPL = 7;                       // digit-plane sets (ring); also keeps one CTA per SM
 constexpr int kScaleRing = 32;               // per-input-plane scale exponents (ring)
 constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 10,368
-constexpr int PAIRS = ST_X / 2, NPAIR = ST_Y * PAIRS;           // 36, 648
-constexpr int PER = (NPAIR + kGroupThreads - 1) / kGroupThreads;  // 6
+// Column pairs of a window row. Only window columns 3..68 meet a nonzero
+// weight (block b reads columns 8b .. 8b+15, taps at k = c+3 .. c+5), so the
+// slicers cut pairs 1..34 (columns 2..69); the digit planes' columns 0, 1, 70
+// and 71 keep the zeros they are initialised with (the MMAs multiply them by
+// zero weights, so they only need to be finite).
+constexpr int PAIRS = ST_X / 2, CUT0 = 1, NCUTX = 34, NCUT = ST_Y * NCUTX;  // 36, 612
+constexpr int PER = (NCUT + kGroupThreads - 1) / kGroupThreads;            // 5
 static_assert(NBLK * NCOL <= kTmemCols, "TMEM blocks exceed the allocation");
 static_assert(kEpiWarps == 8, "two epilogue warps per TMEM lane quarter, four columns each");
 static_assert(kStageBytes % 128 == 0, "TMA destinations stay 128-byte aligned");
@@ -100,9 +105,9 @@ struct Smem {
     unsigned long long blk_full[NBLK], blk_empty[NBLK];
     unsigned tmem;                             // TMEM base column
     int abort;                                 // set by the first expired wait
-    int wait_ok[2][2];                         // slicer group leaders' wait results
+    int wait_ok[kGroups][2];                   // slicer group leaders' wait results
     int scale_exp[kScaleRing];                 // input-plane scale exponents by plane sequence
-    float red[2][kGroupWarps];
+    float red[kGroups][kGroupWarps];
 };
 
 // The MMAs of one input plane: window row offset I, input digit D. `a`
@@ -214,6 +219,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         const __half v = (dz < 3 && tj >= 0 && tj < 3) ? sw.d[e][(dz * 3 + i) * 3 + tj] : __float2half(0.f);
         S.bmat[i][(nn >> 3) * 128 + (nn & 7) * 8 + (k >> 3) * 64 + (k & 7)] = v;
     }
+    for (int i = tid; i < NPL * kDigits * PL / 2; i += kThreads)
+        reinterpret_cast<unsigned *>(&S.planes[0][0][0])[i] = 0u;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
     __syncthreads();
@@ -263,8 +270,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else if (warp < kWarpEpi0) {
         // ------------------------------------------------ slicers
-        // Group grp (four warps) cuts the planes with q % 2 == grp, from
-        // stage buffers grp and grp + 2; the two groups work on consecutive
+        // Group grp (four warps) cuts the planes with q % kGroups == grp, from
+        // stage buffers grp and grp + kGroups; the groups work on consecutive
         // planes at the same time.
         const int grp = (warp - kWarpSlice0) / kGroupWarps, gw = (warp - kWarpSlice0) % kGroupWarps;
         const int st = tid - 32 * (kWarpSlice0 + kGroupWarps * grp);
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int item = first; item < items && go; item += step) {
             const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
             for (int p = 0; p < wi.zn + 2; ++p, ++q) {
-                if ((q & 1) != grp) continue;
+                if (q % kGroups != grp) continue;
                 const int sb = q % kStages, slot = q % NPL;
                 // (a) window landed? One thread waits, the barrier shares the answer.
                 if (leader) S.wait_ok[grp][0] = wait(bar(S.stage_full, sb), (q / kStages) & 1);
@@ -289,10 +296,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 float vmax = 0.f;
 #pragma unroll
                 for (int k = 0; k < PER; ++k) {
-                    const int idx = st + k * kGroupThreads;
+                    const int u = st + k * kGroupThreads;
                     v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (idx < NPAIR) {
-                        v[k] = stg[idx];
+                    if (u < NCUT) {
+                        v[k] = stg[(u / NCUTX) * PAIRS + CUT0 + u % NCUTX];
                         vmax = fmaxf(vmax, fmaxf(fabsf(v[k].x), fabsf(v[k].z)));
                     }
                 }
@@ -318,8 +325,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const float to_digits = ldexpf(1.0f, kDigitBits - ex);
 #pragma unroll
                 for (int k = 0; k < PER; ++k) {
-                    const int idx = st + k * kGroupThreads;
-                    if (idx < NPAIR) {
+                    const int u = st + k * kGroupThreads;
+                    if (u < NCUT) {
+                        const int idx = (u / NCUTX) * PAIRS + CUT0 + u % NCUTX;
                         float d0[kDigits], d1[kDigits];
                         slice_digits(v[k].x * to_digits, v[k].y * to_digits, d0);
                         slice_digits(v[k].z * to_digits, v[k].w * to_digits, d1);
