@@ -360,15 +360,47 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int item = first; item < items && ok; item += step) {
             const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
             const int xb = wi.x0 + 8 * eb + 4 * hh, yy = wi.y0 + er;
-            // Running sums of outputs p - 2 (a) and p - 1 (b), relative to
-            // 2^ea, 2^eb: the largest input-plane scale seen so far for each
-            // (exact powers of two, so only a final product can round into
-            // subnormals).
-            float ah[4], al[4], bh[4], bl[4];
+            // Running sums of outputs p - 2 (a) and p - 1 (b). While every
+            // part added to a sum had the same plane scale (2^ea, 2^eb2), the
+            // sum is kept as level sums: S0, S1, S2 exact (three parts of at
+            // most 45 digit products below 2^16 each stay below 2^24) and the
+            // tail T = S3 2^-27 + S4 2^-36 (its rounding weighs below 2^-50 of
+            // S0's unit); the output is then recombined once. A part with
+            // another scale turns the sum into a (hi, lo) pair in [0], [1]
+            // relative to the largest scale seen (fa, fb set), which takes its
+            // later parts as recombined pairs. Plane scales are the same for
+            // the whole CTA, so the choice never diverges.
+            float a[4][4], b[4][4];
             int ea = 0, eb2 = 0;
-            // Adds a tap plane's part (relative to 2^ex) to a running sum.
-            auto add = [](float (&sh)[4], float (&sl)[4], int &se, const float (&h)[4], const float (&l)[4],
-                          int ex) {
+            bool fa = false, fb = false;
+            auto tail = [](float s3, float s4) { return fmaf(s3, 0x1p-27f, s4 * 0x1p-36f); };
+            // Level sums -> (hi, lo) in [0], [1].
+            auto to_pair = [](float (&sm)[4][4]) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    float h1, e1, h2, e2, hi, lo;
+                    two_sum(sm[0][c], sm[1][c] * 0x1p-9f, h1, e1);
+                    two_sum(h1, sm[2][c] * 0x1p-18f, h2, e2);
+                    two_sum(h2, (e1 + e2) + sm[3][c], hi, lo);
+                    sm[0][c] = hi;
+                    sm[1][c] = lo;
+                }
+            };
+            // Adds a tap plane's part (five levels per column, relative to
+            // 2^ex) to a running sum.
+            auto add_part = [&](float (&sm)[4][4], int &se, bool &fl, const float (&acc)[kDigits][4], int ex) {
+                if (!fl && ex == se) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        sm[0][c] += acc[0][c];
+                        sm[1][c] += acc[1][c];
+                        sm[2][c] += acc[2][c];
+                        sm[3][c] += tail(acc[3][c], acc[4][c]);
+                    }
+                    return;
+                }
+                if (!fl) to_pair(sm);
+                fl = true;
                 float ra = 1.0f, rb = 1.0f;
                 if (ex > se) {
                     ra = ldexpf(1.0f, se - ex);
@@ -378,47 +410,39 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    float s2, e2;
-                    two_sum(sh[c] * ra, h[c] * rb, s2, e2);
-                    sl[c] = sl[c] * ra + (e2 + l[c] * rb);
-                    sh[c] = s2;
+                    float lv[kDigits], ph, pl, s2, e2;
+#pragma unroll
+                    for (int L = 0; L < kDigits; ++L) lv[L] = acc[L][c];
+                    recombine(lv, ph, pl);
+                    two_sum(sm[0][c] * ra, ph * rb, s2, e2);
+                    sm[1][c] = sm[1][c] * ra + (e2 + pl * rb);
+                    sm[0][c] = s2;
                 }
+            };
+            auto load_part = [&](int q, int dz, float (&acc)[kDigits][4]) {
+                const unsigned col = (unsigned)(NCOL * (q % NBLK) + 8 * dz + 4 * hh);
+#pragma unroll
+                for (int L = 0; L < kDigits; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
+                tmem_wait_ld();
             };
             for (int p = 0; p < wi.zn + 2; ++p) {
                 const int q = q0 + p;
                 if (!(ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1))) break;
                 tc_fence_after();
                 const int ex = S.scale_exp[q % kScaleRing];
-                float ph[3][4], pl[3][4];  // recombined (hi, lo) per z tap
-#pragma unroll
-                for (int dz = 0; dz < 3; ++dz) {
-                    const unsigned col = (unsigned)(NCOL * (q % NBLK) + 8 * dz + 4 * hh);
-                    float acc[kDigits][4];
-#pragma unroll
-                    for (int L = 0; L < kDigits; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        float lv[kDigits];
-#pragma unroll
-                        for (int L = 0; L < kDigits; ++L) lv[L] = acc[L][c];
-                        recombine(lv, ph[dz][c], pl[dz][c]);
-                    }
-                }
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(bar(S.blk_empty, q % NBLK));
-                // z tap 2 of output p - 2 (its last: store), 1 of output p - 1,
-                // 0 of output p (its first).
+                float acc[kDigits][4];
+                // z tap 2 of output p - 2: its last part; store.
+                load_part(q, 2, acc);
                 if (p >= 2) {
-                    add(ah, al, ea, ph[2], pl[2], ex);
+                    add_part(a, ea, fa, acc, ex);
+                    if (!fa) to_pair(a);
                     if (yy < m) {
                         const float scale = ldexpf(1.0f, ea + sw.ew - 2 * kDigitBits);
                         float2 res[4];
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {
                             float hi, lo;
-                            two_sum(ah[c], al[c], hi, lo);
+                            two_sum(a[0][c], a[1][c], hi, lo);
                             res[c] = make_float2(hi * scale, lo * scale);
                         }
                         float2 *op = out + (long long)(wi.zs + p - 2) * ldz + (long long)yy * ldy + xb;
@@ -432,14 +456,28 @@ __global__ void __launch_bounds__(kThreads, 1)
                         }
                     }
                 }
-                if (p >= 1 && p - 1 < wi.zn) add(bh, bl, eb2, ph[1], pl[1], ex);
+                // z tap 1 of output p - 1.
+                load_part(q, 1, acc);
+                if (p >= 1 && p - 1 < wi.zn) add_part(b, eb2, fb, acc, ex);
+                // z tap 0 of output p: its first part. The block is then
+                // drained and handed back.
+                load_part(q, 0, acc);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(S.blk_empty, q % NBLK));
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {  // rotate: p - 1 becomes p - 2, p starts
-                    ah[c] = bh[c], al[c] = bl[c];
-                    bh[c] = ph[0][c], bl[c] = pl[0][c];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) a[k][c] = b[k][c];
+                    b[0][c] = acc[0][c];
+                    b[1][c] = acc[1][c];
+                    b[2][c] = acc[2][c];
+                    b[3][c] = tail(acc[3][c], acc[4][c]);
                 }
                 ea = eb2;
+                fa = fb;
                 eb2 = ex;
+                fb = false;
             }
             q0 += wi.zn + 2;
         }
