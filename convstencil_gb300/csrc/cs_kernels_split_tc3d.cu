@@ -31,14 +31,18 @@
 //     columns 0, 160, 320), so every plane keeps its own scale. The epilogue
 //     reads a block once, as soon as its MMAs are done, hands it back, and
 //     adds its three tap-plane parts to the running sums of output planes
-//     P+1 (dz = 0), P (dz = 1) and P-1 (dz = 2, its last: stored).
-//   * Roles: one warp issues the window loads (four stage buffers), one
-//     thread issues the MMAs, two groups of four warps cut alternate input
-//     planes into digit planes (ring of seven; a plane is too small for
-//     eight warps to share without waiting on each other),
-//     eight warps (a TMEM lane quarter and half of the 8 columns each)
-//     recombine each plane's levels, add the three double-float partial sums
-//     of an output relative to the largest plane scale, scale once and store.
+//     P+1 (dz = 0), P (dz = 1) and P-1 (dz = 2, its last: stored). Parts of
+//     one output with the same plane scale (the usual case) are added as
+//     exact level sums and recombined once; otherwise as (hi, lo) pairs
+//     relative to the largest scale.
+//   * Roles: one warp issues the window loads (six stage buffers), one
+//     thread issues the MMAs, three groups of four warps cut every third
+//     input plane into digit planes (ring of seven; a plane is too small for
+//     many warps to share without waiting on each other; only the window
+//     columns that meet nonzero weights are cut), and eight warps (a TMEM
+//     lane quarter and half of the 8 columns each) drain the blocks,
+//     recombine, scale once and store. No slicer shares the MMA thread's
+//     warp scheduler.
 //
 // Every mbarrier wait is bounded (WaitCfg, 2 s by default). An expired wait is
 // counted in g_tc3d_wait_timeouts; the CTA then waits, again bounded, for the
@@ -63,12 +67,28 @@ using split::slice_digits;
 using split::two_sum;
 using namespace tc;
 
-// Warp roles.
+// Warp roles. Warp w issues from the SM's scheduler w % 4, and an epilogue
+// warp can read only TMEM lanes 32 (w % 4) .. + 31, so each scheduler hosts
+// two epilogue warps. The MMA thread stalls on every tcgen05.mma until the
+// tensor core takes it, so every issue slot it loses to a busy neighbour
+// stretches the MMA stream: it shares scheduler 1 with the TMA warp, the two
+// epilogue warps of lane quarter 1 and two idle warps, and the twelve slicer
+// warps sit on schedulers 0, 2 and 3 (box3d1r 512^3 on GB300: 135 -> 148
+// GStencil/s against slicers spread over all four). 24 warps, six per
+// scheduler, leave 80 registers a thread.
 constexpr int kGroups = 3, kGroupWarps = 4;  // slicer groups of four warps take every third plane
 constexpr int kSliceWarps = kGroups * kGroupWarps, kEpiWarps = 8;
-constexpr int kWarpTma = 0, kWarpMma = 1, kWarpSlice0 = 2, kWarpEpi0 = kWarpSlice0 + kSliceWarps;
-constexpr int kThreads = 32 * (kWarpEpi0 + kEpiWarps);  // 704
+constexpr int kWarpTma = 1, kWarpMma = 5;
+constexpr unsigned kEpiMask = (1u << 0) | (1u << 2) | (1u << 3) | (1u << 4) | (1u << 6) | (1u << 7) | (1u << 9) |
+                              (1u << 13);
+constexpr unsigned kSliceMask = (1u << 8) | (1u << 10) | (1u << 11) | (1u << 12) | (1u << 14) | (1u << 15) |
+                                (1u << 16) | (1u << 18) | (1u << 19) | (1u << 20) | (1u << 22) | (1u << 23);
+constexpr int kThreads = 32 * 24;  // warps 17 and 21 idle
 constexpr int kGroupThreads = 32 * kGroupWarps;
+static_assert(__builtin_popcount(kSliceMask) == kSliceWarps && __builtin_popcount(kEpiMask) == kEpiWarps &&
+                  (kSliceMask & kEpiMask) == 0 && ((kSliceMask | kEpiMask) & ((1u << kWarpTma) | (1u << kWarpMma))) == 0,
+              "warp roles overlap");
+static_assert((kSliceMask & 0x22222222u) == 0 && (kWarpMma & 3) == 1, "no slicer beside the MMA thread");
 constexpr int kSliceBarrier = 1;             // named barriers 1 .. kGroups: one per slicer group
 
 constexpr int G = 16;                        // output rows per tile (M = G x 8 blocks = 128)
@@ -268,13 +288,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
             }
         }
-    } else if (warp < kWarpEpi0) {
+    } else if ((kSliceMask >> warp) & 1u) {
         // ------------------------------------------------ slicers
         // Group grp (four warps) cuts the planes with q % kGroups == grp, from
         // stage buffers grp and grp + kGroups; the groups work on consecutive
         // planes at the same time.
-        const int grp = (warp - kWarpSlice0) / kGroupWarps, gw = (warp - kWarpSlice0) % kGroupWarps;
-        const int st = tid - 32 * (kWarpSlice0 + kGroupWarps * grp);
+        const int sidx = __popc(kSliceMask & ((1u << warp) - 1u));  // 0 .. kSliceWarps - 1
+        const int grp = sidx / kGroupWarps, gw = sidx % kGroupWarps;
+        const int st = 32 * gw + lane;
         const bool leader = st == 0;
         int q = 0;
         bool go = true;
@@ -342,16 +363,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (lane == 0) mbar_arrive(bar(S.planes_full, slot));
             }
         }
-    } else {
+    } else if ((kEpiMask >> warp) & 1u) {
         // ------------------------------------------------ epilogue
         // Warp w reads TMEM lanes 32 (w % 4) ..; lane -> D row m = (output
-        // row er, block eb); warp half hh takes columns 8 eb + 4 hh .. + 3.
+        // row er, block eb); of the two warps of a lane quarter (w < 4 and
+        // w >= 4 for quarters 0, 2, 3; 9 and 13 for quarter 1) hh = 0, 1
+        // takes columns 8 eb + 4 hh .. + 3.
         // Each input plane's block is read once, as soon as its MMAs are
         // done, and handed back at once: its three tap-plane partial sums go
         // to the running sums of the output planes it feeds. Output j of the
         // column receives input plane j (dz = 0), j+1 (dz = 1) and j+2
         // (dz = 2) in that order and is stored after the last.
-        const int quarter = warp & 3, hh = (warp - kWarpEpi0) >> 2;
+        const int quarter = warp & 3, hh = (warp >> 2) & 1;
         const int mrow = 32 * quarter + lane;
         const int er = mrow >> 3, eb = mrow & 7;
         const unsigned lane_bits = (unsigned)(32 * quarter) << 16;
