@@ -54,8 +54,8 @@
 //     window loads, one thread issues the MMAs (tcgen05.mma issue blocks
 //     while the tensor core is busy, so it must not sit in anyone else's
 //     barrier), eight warps read a window into registers, release the stage
-//     to the next load and cut the digit planes, and eight warps drain the
-//     accumulators, recombine and store. Two accumulators (TMEM columns 0 and
+//     to the next load and cut the digit planes, and four (split) or eight
+//     (FP64) warps drain the accumulators, recombine and store. Two accumulators (TMEM columns 0 and
 //     256) and two sets of digit planes let slicing of tile t+1, the MMAs of
 //     tile t and the stores of tile t-1 run at the same time.
 //
@@ -87,9 +87,15 @@ using split::two_sum;
 using namespace tc;
 
 // Number formats.
+// kEpiWarps: epilogue warps, one or two per TMEM lane quarter. Every warp the
+// epilogue runs takes issue slots from the slicers, which bound the split
+// kernel, so its light recombination runs on four warps (8192^2 on GB300:
+// 192 -> 204 GStencil/s against eight); the FP64 recombination (integer
+// operations) needs eight (120 GStencil/s on four, 169 on eight).
 struct FmtSplit {
     static constexpr bool kF64 = false;
     static constexpr int kDigits = split::kDigits;  // 5
+    static constexpr int kEpiWarps = 4;
     using Out = float2;
     using Digits = split::SliceWeights;
 };
@@ -104,6 +110,7 @@ struct F64Weights {
 struct FmtF64 {
     static constexpr bool kF64 = true;
     static constexpr int kDigits = 6;
+    static constexpr int kEpiWarps = 8;
     using Out = double;
     using Digits = F64Weights;
 };
@@ -210,9 +217,10 @@ __device__ __forceinline__ double f64_from_fixed(long long t, int c)
 constexpr int kNonFiniteTile = -100000;
 
 // Warp roles.
-constexpr int kSliceWarps = 8, kEpiWarps = 8;
+constexpr int kSliceWarps = 8;
 constexpr int kWarpTma = 0, kWarpMma = 1, kWarpSlice0 = 2, kWarpEpi0 = kWarpSlice0 + kSliceWarps;
-constexpr int kThreads = 32 * (kWarpEpi0 + kEpiWarps);  // 576
+template <class F>
+constexpr int kThreads = 32 * (kWarpEpi0 + F::kEpiWarps);  // 448 split, 576 FP64
 constexpr int kSliceThreads = 32 * kSliceWarps;
 constexpr int kSliceBarrier = 1;           // named barrier of the slicer warps
 
@@ -229,7 +237,8 @@ constexpr int kTmemCols = 512;
 constexpr unsigned kStageBytes = ST_X * ST_Y * 8;  // 40,320 (8-byte points)
 constexpr int PAIRS = ST_X / 2, NPAIR = ST_Y * PAIRS;           // 36, 2,520
 constexpr int PER = (NPAIR + kSliceThreads - 1) / kSliceThreads;  // 10
-static_assert(kEpiWarps == 2 * 4 && R == 4, "two epilogue warps per TMEM lane quarter, two rows each");
+static_assert(FmtSplit::kEpiWarps == 4 && FmtF64::kEpiWarps == 8 && R == 4,
+              "one or two epilogue warps per TMEM lane quarter, R / (warps per quarter) rows each");
 
 template <class F>
 struct Smem {
@@ -319,7 +328,7 @@ __device__ __forceinline__ int grid_of(const TcGrid<F> *grids, int ngrids, int t
 // rebuilds its B matrices when the run crosses into the next grid, after
 // the MMAs of the previous tile have completed).
 template <class F, bool BATCH>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads<F>, 1)
     k2d_tc(const __grid_constant__ CUtensorMap tmap, typename F::Out *__restrict__ out, int m, int n,
            long long ld, int tiles_x, int tiles, int map_x, int map_y, typename F::Digits sw, WaitCfg wc,
            const TcGrid<F> *__restrict__ grids, int ngrids)
@@ -383,7 +392,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(bar2(S.planes_full, i), kSliceWarps);
             mbar_init(bar2(S.planes_empty, i), 1);
             mbar_init(bar2(S.acc_full, i), 1);
-            mbar_init(bar2(S.acc_empty, i), kEpiWarps);
+            mbar_init(bar2(S.acc_empty, i), F::kEpiWarps);
         }
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -405,10 +414,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (my_tiles > 0) {
             int x0, y0;
             tile_at(0, g_bmat, x0, y0);
-            build_bmat<F>(S, grids[g_bmat].digits, tid, kThreads);
+            build_bmat<F>(S, grids[g_bmat].digits, tid, kThreads<F>);
         }
     } else {
-        build_bmat<F>(S, sw, tid, kThreads);
+        build_bmat<F>(S, sw, tid, kThreads<F>);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
@@ -566,8 +575,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
         // ------------------------------------------------ epilogue
         // Warp w reads TMEM lanes 32 (w % 4) ..; lane -> D row m = (row group
-        // er, block eb); the two warps of a quarter store rows 2h, 2h+1 of the
-        // group, columns 8 eb .. 8 eb + 7.
+        // er, block eb); warp h of a quarter (one warp per quarter split,
+        // two FP64) stores rows kRowsPerWarp h .. of the group, columns
+        // 8 eb .. 8 eb + 7.
         const int quarter = warp & 3, h = (warp - kWarpEpi0) >> 2;
         const int mrow = 32 * quarter + lane;
         const int er = mrow >> 3, eb = mrow & 7;
@@ -590,15 +600,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             const int ex = S.scale_exp[it & 3];
             const int xb = x0 + 8 * eb;
+            constexpr int kRowsPerWarp = R * 4 / F::kEpiWarps;  // 4 split, 2 FP64
 #pragma unroll 1
-            for (int pass = 0; pass < 2; ++pass) {
-                const int rho = 2 * h + pass;
+            for (int pass = 0; pass < kRowsPerWarp; ++pass) {
+                const int rho = kRowsPerWarp * h + pass;
                 float acc[D][8];
 #pragma unroll
                 for (int L = 0; L < D; ++L)
                     tmem_ld8(tmem + lane_bits + (unsigned)(kAccStride * buf + NLV * L + 8 * rho), acc[L]);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (pass == 1) {  // accumulator drained: hand it back to the MMA warp
+                if (pass == kRowsPerWarp - 1) {  // accumulator drained: hand it back to the MMA warp
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(bar2(S.acc_empty, buf));
@@ -690,7 +701,7 @@ cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long 
     // the TMEM allocation never waits).
     const int grid = std::min(tiles, device_sm_count());
     note_launch();
-    k2d_tc<F, false><<<grid, kThreads, sizeof(Smem<F>) + 128, st>>>(
+    k2d_tc<F, false><<<grid, kThreads<F>, sizeof(Smem<F>) + 128, st>>>(
         map, reinterpret_cast<typename F::Out *>(out_base) + origin, (int)g.ext[0], (int)g.ext[1], ld, tiles_x,
         tiles, (int)(origin % ld), (int)(origin / ld), digits, wc, nullptr, 0);
     return cudaGetLastError();
@@ -730,7 +741,7 @@ cudaError_t launch_batch(const void *records, int ngrids, int total, const WaitC
     std::memset(&unused, 0, sizeof unused);
     const int grid = std::min(total, device_sm_count());
     note_launch();
-    k2d_tc<F, true><<<grid, kThreads, sizeof(Smem<F>) + 128, st>>>(
+    k2d_tc<F, true><<<grid, kThreads<F>, sizeof(Smem<F>) + 128, st>>>(
         unused, nullptr, 0, 0, 0, 0, total, 0, 0, typename F::Digits{}, wc,
         reinterpret_cast<const TcGrid<F> *>(records), ngrids);
     return cudaGetLastError();
