@@ -559,12 +559,15 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
                 for (int q = 0; q < PER; ++q) {
                     const int idx = st + q * kSliceThreads;
                     if (idx < NPAIR) {
-                        float d0[D], d1[D];
-                        slice_digits(__uint_as_float(v[q].x) * to_digits, __uint_as_float(v[q].y) * to_digits, d0);
-                        slice_digits(__uint_as_float(v[q].z) * to_digits, __uint_as_float(v[q].w) * to_digits, d1);
+                        split::f2x a, b, s2;
+                        asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "r"(v[q].x), "r"(v[q].z));
+                        asm("mov.b64 %0, {%1, %2};" : "=l"(b) : "r"(v[q].y), "r"(v[q].w));
+                        asm("mov.b64 %0, {%1, %1};" : "=l"(s2) : "f"(to_digits));
+                        unsigned wd[D];
+                        split::slice_digit_pairs_x2(split::f2_mul(a, s2), split::f2_mul(b, s2), wd);
                         unsigned *dst = dst0 + idx;
 #pragma unroll
-                        for (int k = 0; k < D; ++k) dst[k * (PL / 2)] = split::pack_h2(d0[k], d1[k]);
+                        for (int k = 0; k < D; ++k) dst[k * (PL / 2)] = wd[k];
                     }
                 }
             }

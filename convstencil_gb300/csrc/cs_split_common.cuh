@@ -95,6 +95,37 @@ __device__ __forceinline__ void slice_digits(float a, float b, float (&d)[kDigit
     d[kDigits - 1] = rintf(a + b);
 }
 
+// The digits of slice_digits for two points (a0 + b0, a1 + b1) at once, as
+// FP16 pairs (first point in the low half), on packed FP32 pair
+// instructions. rint(s) is taken as (s + M) - M with M = 1.5 * 2^23 + 512:
+// for |s| < 2^22, s + M lies in [2^23, 2^24), where the FP32 spacing is 1,
+// so it rounds to M + rint(s) exactly (M is even, so ties go to the same
+// even integer as rint), and its low 10 mantissa bits hold 512 + d (256..768
+// for |d| <= 256). FP16 (1024 + u) has the bits 0x6400 | u, so a byte
+// permute and a mask-and-or build both halves, and one FP16 subtraction of
+// 1536 leaves the digits exactly. Each lane of a pair instruction rounds as
+// the scalar one, so the digits equal slice_digits' (a zero digit is +0).
+__device__ __forceinline__ void slice_digit_pairs_x2(f2x a, f2x b, unsigned (&w)[kDigits])
+{
+    const f2x m2 = 0x4B4002004B400200ull;  // (M, M)
+    const f2x r2 = 0x4400000044000000ull;  // (512, 512)
+    const __half2 bias = __halves2half2(__ushort_as_half(0x6600), __ushort_as_half(0x6600));  // 1536
+#pragma unroll
+    for (int k = 0; k < kDigits; ++k) {
+        const f2x t = f2_add(f2_add(a, b), m2);
+        unsigned t0, t1, u;
+        asm("mov.b64 {%0, %1}, %2;" : "=r"(t0), "=r"(t1) : "l"(t));
+        asm("prmt.b32 %0, %1, %2, 0x5410;" : "=r"(u) : "r"(t0), "r"(t1));
+        u = (u & 0x03FF03FFu) | 0x64006400u;
+        const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&u), bias);
+        w[k] = *reinterpret_cast<const unsigned *>(&h);
+        if (k + 1 < kDigits) {
+            a = f2_mul(f2_sub(a, f2_sub(t, m2)), r2);
+            b = f2_mul(b, r2);
+        }
+    }
+}
+
 // Scale exponent of a tile from the largest |hi| in its window: every
 // |x| / 2^ex < 1/2. Clamped below at -110 so that the slicing factor
 // 2^(kDigitBits - ex) stays finite in FP32; a tile whose values are all below
