@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
     extern __shared__ unsigned char smem_raw[];
     SM &S = *reinterpret_cast<SM *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    pdl_allow_dependents();
     int my_tiles, first = 0;
     if constexpr (BATCH) {
         const int per = tiles / (int)gridDim.x, extra = tiles % (int)gridDim.x, b = (int)blockIdx.x;
@@ -397,6 +398,7 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (my_tiles > 0 && !wc.skip_loads) {  // the first window load overlaps the set-up below
+            pdl_wait();
             load_window(0, stage_full);
             issued = 1;
         }
@@ -704,10 +706,10 @@ cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long 
     // the TMEM allocation never waits).
     const int grid = std::min(tiles, device_sm_count());
     note_launch();
-    k2d_tc<F, false><<<grid, kThreads<F>, sizeof(Smem<F>) + 128, st>>>(
-        map, reinterpret_cast<typename F::Out *>(out_base) + origin, (int)g.ext[0], (int)g.ext[1], ld, tiles_x,
-        tiles, (int)(origin % ld), (int)(origin / ld), digits, wc, nullptr, 0);
-    return cudaGetLastError();
+    return launch_programmatic(k2d_tc<F, false>, grid, kThreads<F>, sizeof(Smem<F>) + 128, st, map,
+                               reinterpret_cast<typename F::Out *>(out_base) + origin, (int)g.ext[0],
+                               (int)g.ext[1], ld, tiles_x, tiles, (int)(origin % ld), (int)(origin / ld), digits,
+                               wc, static_cast<const TcGrid<F> *>(nullptr), 0);
 }
 
 template <class F>

@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     Smem &S = *reinterpret_cast<Smem *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    pdl_allow_dependents();
     volatile int *abort = &S.abort;
     auto bar = [](unsigned long long *b, int i) { return smem_addr(&b[i]); };
     const unsigned long long limit = wc.limit_ns;
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
         if (lane == 0 && !wc.skip_loads) {
+            pdl_wait();  // the previous sweep has finished with both buffers
             int q = 0;  // input-plane sequence number
             bool ok = true;
             for (int item = first; item < items && ok; item += step) {
@@ -565,11 +567,9 @@ cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long lo
     const int items = (int)(txy * ((h + zc - 1) / zc));
     const int grid = std::min(items, sms);
     note_launch();
-    k3d_tc<<<grid, kThreads, smem, st>>>(map, out_base + origin, h, m, n, ldy, ldz, tiles_x, tiles_y, zc,
-                                        items, (int)(origin % ldy), (int)((origin % ldz) / ldy),
-                                        (int)(origin / ldz), split::slice_weights(w, 27),
-                                        WaitCfg{wt.limit_ns, wt.skip_loads});
-    return cudaGetLastError();
+    return launch_programmatic(k3d_tc, grid, kThreads, smem, st, map, out_base + origin, h, m, n, ldy, ldz, tiles_x,
+                               tiles_y, zc, items, (int)(origin % ldy), (int)((origin % ldz) / ldy),
+                               (int)(origin / ldz), split::slice_weights(w, 27), WaitCfg{wt.limit_ns, wt.skip_loads});
 }
 
 cudaError_t split_tc3d_wait_timeouts(unsigned *count, bool reset)

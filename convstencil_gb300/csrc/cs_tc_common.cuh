@@ -13,6 +13,9 @@
 
 #include <cuda.h>
 #include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <utility>
 
 namespace cs {
 namespace tc {
@@ -25,6 +28,39 @@ struct WaitCfg {
     int skip_loads;               // test hook: the producer issues no TMA loads, so the
                                   // consumers' first wait runs out and the CTA leaves
 };
+
+// Programmatic dependent launch. A sweep launched with the programmatic
+// stream serialization attribute may be scheduled while the previous kernel
+// of its stream is still finishing: it sets up (barriers, TMEM, B matrices)
+// at once and calls pdl_wait(), which returns once the previous grid has
+// completed and its writes are visible, before its first global-memory
+// access (the first window load; every store comes after loads). Launched
+// without the attribute, pdl_wait() returns at once. pdl_allow_dependents()
+// lets the next such kernel be scheduled as this one's CTAs leave.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_allow_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches a sweep kernel with the programmatic stream serialization
+// attribute (see pdl_wait).
+template <typename... Exp, typename... Act>
+cudaError_t launch_programmatic(void (*kernel)(Exp...), int grid, int block, size_t smem, cudaStream_t st,
+                                Act &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
+}
 
 __device__ __forceinline__ unsigned smem_addr(const void *p)
 {
