@@ -242,12 +242,27 @@ struct cs_plan {
     std::mutex host_mu;
     void *host_bufs[2] = {nullptr, nullptr};
     size_t host_bytes = 0;
+    // The band schedule of host-buffer runs on the tcgen05 batch kernel
+    // (host_run_banded): the device records of every distinct set of
+    // band-sweeps, kept for the bands, sweeps and grids they were made for.
+    struct BandSet {
+        long long rec;  // first record in the table
+        int count, tiles;
+    };
+    struct BandTable {
+        int bands = 0, algo = -1;
+        long long sweeps = 0;
+        const void *d0 = nullptr, *d1 = nullptr;
+        void *tab = nullptr;
+        std::vector<BandSet> sets;  // one per set, in launch order
+    } band;
     ~cs_plan()
     {
         for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
         if (capture_stream) cudaStreamDestroy(capture_stream);
         for (void *b : host_bufs)
             if (b) cudaFree(b);
+        if (band.tab) cudaFree(band.tab);
     }
 };
 
@@ -950,6 +965,17 @@ struct DevBuf {
 // overwrites rows that it reads. Used when the kernel is known without a
 // timing run, no temporal blocking and no re-anchor sweep is involved, and
 // the whole grid goes both ways.
+// Whether the band-sweeps of a host-buffer run go to the tcgen05 batch
+// kernel: 2D split plans on SPLIT_TC (the 2D radius-3 tile geometry). On
+// GB300, 20 sweeps of 8192^2 with the copies: 10.3 ms in 32 bands of batched
+// sets against 11.7 in 8 bands of one launch each; FP64 plans gain nothing
+// from the batches (12.1 against 11.9 ms), whose kernel runs 5 % slower than
+// the one-grid kernel, and keep one launch per band-sweep.
+bool band_batch_ok(const cs_plan *p, int algo)
+{
+    return p->prec == CS_PREC_SPLIT && algo == CS_ALGO_SPLIT_TC && fp64_tc_geometry_ok(p);
+}
+
 bool banded_ok(cs_plan *p, long long sweeps, int *algo, int *bands)
 {
     if (p->dims < 2 || sweeps < 1) return false;
@@ -958,9 +984,85 @@ bool banded_ok(cs_plan *p, long long sweeps, int *algo, int *bands)
     if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && sweeps >= p->reanchor) return false;
     if (choose_algo(p, nullptr, nullptr, nullptr, algo, false) != CS_OK || *algo < 0) return false;
     const long long slabs = p->view.ext[0];
-    const long long per = p->dims == 2 ? 1024 : 64;  // slabs per band at least
-    *bands = (int)std::min<long long>(8, slabs / per);
+    if (band_batch_ok(p, *algo)) {
+        *bands = (int)std::min<long long>(32, slabs / 256);  // one batch launch per set
+    } else {
+        const long long per = p->dims == 2 ? 1024 : 64;  // slabs per band at least
+        *bands = (int)std::min<long long>(8, slabs / per);
+    }
     return *bands >= 2;
+}
+
+// Band-sweep (k, s) is sweep s (0-based) of the interior slabs of band k: it
+// reads level s of bands k-1 .. k+1 (grid s % 2) and writes level s+1 of band
+// k (grid (s+1) % 2). Its inputs come from (k-1, s-1), (k, s-1), (k+1, s-1),
+// and the level s-1 it overwrites was last read by the same three, so with
+// c = 2s + k every dependency points from set c to sets c-1, c-2, c-3: the
+// band-sweeps of one set are independent (neighbouring bands are never in
+// the same set, and bands are taller than the halo), and the sets in order
+// c = 0, 1, ... form a wavefront that starts on the first bands while later
+// ones are still arriving. Set c needs band c + 1 on the device when c < K.
+struct BandMember {
+    int k;
+    long long s;
+};
+static std::vector<BandMember> band_set(int bands, long long sweeps, long long c)
+{
+    std::vector<BandMember> m;
+    for (long long sw = std::max(0LL, (c - bands + 2) / 2); sw <= std::min(sweeps - 1, c / 2); ++sw) {
+        const long long k = c - 2 * sw;
+        if (k >= 0 && k < bands) m.push_back({(int)k, sw});
+    }
+    return m;
+}
+
+// The batch records of every set (sets whose members have the same bands
+// and grid parities share them: in the middle of a long run the pattern
+// repeats every four sets), uploaded once per bands, sweeps and grids.
+static cs_status band_table(cs_plan *p, int algo, int bands, long long sweeps, void *const d[2],
+                            const std::vector<long long> &b)
+{
+    auto &T = p->band;
+    if (T.tab && T.bands == bands && T.sweeps == sweeps && T.algo == algo && T.d0 == d[0] && T.d1 == d[1])
+        return CS_OK;
+    if (T.tab) cudaFree(T.tab), T.tab = nullptr;
+    T.sets.clear();
+    const bool fp64 = p->prec == CS_PREC_FP64;
+    const size_t rb = cs::tc_batch_record_bytes(fp64);
+    std::vector<unsigned char> rec;
+    std::map<std::vector<long long>, cs_plan::BandSet> seen;
+    const long long nsets = 2 * (sweeps - 1) + bands;
+    for (long long c = 0; c < nsets; ++c) {
+        const auto mem = band_set(bands, sweeps, c);
+        std::vector<long long> sig;
+        for (const auto &x : mem) sig.push_back(2 * x.k + (x.s & 1));
+        auto it = seen.find(sig);
+        if (it == seen.end()) {
+            cs_plan::BandSet bs{(long long)(rec.size() / rb), (int)mem.size(), 0};
+            for (const auto &x : mem) {
+                GridView v = p->view;
+                v.ext[0] = b[x.k + 1] - b[x.k];
+                const long long off = p->layout.origin + b[x.k] * p->view.pitch[0];
+                rec.resize(rec.size() + rb);
+                int tiles = 0;
+                const cudaError_t e = cs::tc_batch_fill_record(fp64, rec.data() + rec.size() - rb, v, p->w, off,
+                                                               p->layout.elements, d[x.s & 1], d[(x.s + 1) & 1],
+                                                               bs.tiles, 0, &tiles);
+                if (e != cudaSuccess) return fail(CS_ERR_CUDA, "band record: %s", cudaGetErrorString(e));
+                bs.tiles += tiles;
+            }
+            it = seen.emplace(sig, bs).first;
+        }
+        T.sets.push_back(it->second);
+    }
+    CS_CUDA(cudaMalloc(&T.tab, rec.size()));
+    CS_CUDA(cudaMemcpy(T.tab, rec.data(), rec.size(), cudaMemcpyHostToDevice));
+    T.bands = bands;
+    T.sweeps = sweeps;
+    T.algo = algo;
+    T.d0 = d[0];
+    T.d1 = d[1];
+    return CS_OK;
 }
 
 cs_status host_run_banded(cs_plan *p, int algo, int bands, const double *host_in, double *host_out,
@@ -976,6 +1078,20 @@ cs_status host_run_banded(cs_plan *p, int algo, int bands, const double *host_in
     b[bands] = slabs;
     std::vector<long long> c(bands + 1);  // buffer slab boundaries of the copy chunks
     for (int k = 0; k <= bands; ++k) c[k] = k == 0 ? 0 : k == bands ? total : first + b[k];
+    // The tcgen05 batch kernel takes a whole set per launch when every band
+    // meets its layout conditions; otherwise each band-sweep is a launch.
+    bool batch = band_batch_ok(p, algo) && reinterpret_cast<uintptr_t>(d[0]) % 16 == 0 &&
+                 reinterpret_cast<uintptr_t>(d[1]) % 16 == 0;
+    for (int k = 0; k < bands && batch; ++k) {
+        GridView v = p->view;
+        v.ext[0] = b[k + 1] - b[k];
+        const long long off = p->layout.origin + b[k] * ld0;
+        batch = cs::split_tma_layout_ok(v, off, d[0]) && cs::split_tma_layout_ok(v, off, d[1]);
+    }
+    if (batch) {
+        const cs_status st = band_table(p, algo, bands, sweeps, d, b);
+        if (st != CS_OK) return st;
+    }
     struct Streams {
         cudaStream_t s[3] = {nullptr, nullptr, nullptr};
         std::vector<cudaEvent_t> ev;
@@ -1002,22 +1118,45 @@ cs_status host_run_banded(cs_plan *p, int algo, int bands, const double *host_in
     }
     CS_CUDA(cudaEventRecord(e0, sc));
     void *f = d[sweeps & 1];  // final grid
-    for (long long diag = 0; diag < bands + sweeps - 1; ++diag) {
-        for (long long sw = std::max(0LL, diag - (bands - 1)); sw <= std::min(sweeps - 1, diag); ++sw) {
-            const int k = (int)(diag - sw);
-            if (sw == 0) {
-                CS_CUDA(cudaStreamWaitEvent(sc, in_ev[k], 0));
-                if (k + 1 < bands) CS_CUDA(cudaStreamWaitEvent(sc, in_ev[k + 1], 0));
-            }
-            CS_CUDA(launch_sweep_rows(p, algo, d[sw & 1], d[(sw + 1) & 1], b[k], b[k + 1] - b[k], sc));
-            if (sw == sweeps - 1) {  // band k is final: back to the host now
-                const long long cnt = (c[k + 1] - c[k]) * ld0;
-                char *src = (char *)f + c[k] * slab_bytes;
-                if (p->prec == CS_PREC_SPLIT) CS_CUDA(cs::launch_split_to_fp64_inplace(cnt, src, sc));
-                CS_CUDA(cudaEventRecord(out_ev[k], sc));
-                CS_CUDA(cudaStreamWaitEvent(sd, out_ev[k], 0));
-                CS_CUDA(cudaMemcpyAsync(host_out + c[k] * ld0, src, (size_t)cnt * sizeof(double),
-                                        cudaMemcpyDeviceToHost, sd));
+    const bool fp64 = p->prec == CS_PREC_FP64;
+    const size_t rb = batch ? cs::tc_batch_record_bytes(fp64) : 0;
+    auto band_done = [&](int k) -> cs_status {  // band k is final: back to the host now
+        const long long cnt = (c[k + 1] - c[k]) * ld0;
+        char *src = (char *)f + c[k] * slab_bytes;
+        if (p->prec == CS_PREC_SPLIT) CS_CUDA(cs::launch_split_to_fp64_inplace(cnt, src, sc));
+        CS_CUDA(cudaEventRecord(out_ev[k], sc));
+        CS_CUDA(cudaStreamWaitEvent(sd, out_ev[k], 0));
+        CS_CUDA(cudaMemcpyAsync(host_out + c[k] * ld0, src, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, sd));
+        return CS_OK;
+    };
+    if (batch) {
+        // One batch launch per set c = 2s + k (band_set).
+        const long long nsets = 2 * (sweeps - 1) + bands;
+        for (long long set = 0; set < nsets; ++set) {
+            // Bands arrive in order on one stream: band set + 1 implies the rest.
+            if (set < bands) CS_CUDA(cudaStreamWaitEvent(sc, in_ev[std::min<long long>(set + 1, bands - 1)], 0));
+            const cs_plan::BandSet &bs = p->band.sets[set];
+            CS_CUDA(cs::launch_tc_batch(fp64, (const char *)p->band.tab + bs.rec * rb, bs.count, bs.tiles, p->wait,
+                                        sc));
+            for (const auto &x : band_set(bands, sweeps, set))
+                if (x.s == sweeps - 1) {
+                    const cs_status st = band_done(x.k);
+                    if (st != CS_OK) return st;
+                }
+        }
+    } else {
+        // One launch per band-sweep, diagonal by diagonal (d = k + s): a
+        // topological order too, with (k, s) launched before (k - 1, s + 1),
+        // which overwrites the rows it reads; (k, 0) waits for bands k, k + 1.
+        for (long long diag = 0; diag < bands + sweeps - 1; ++diag) {
+            for (long long sw = std::max(0LL, diag - (bands - 1)); sw <= std::min(sweeps - 1, diag); ++sw) {
+                const int k = (int)(diag - sw);
+                if (sw == 0) CS_CUDA(cudaStreamWaitEvent(sc, in_ev[std::min(k + 1, bands - 1)], 0));
+                CS_CUDA(launch_sweep_rows(p, algo, d[sw & 1], d[(sw + 1) & 1], b[k], b[k + 1] - b[k], sc));
+                if (sw == sweeps - 1) {
+                    const cs_status st = band_done(k);
+                    if (st != CS_OK) return st;
+                }
             }
         }
     }

@@ -22,6 +22,7 @@
 #include "cs_split_ff.cuh"
 
 #include <algorithm>
+#include <cstring>
 #include <climits>
 #include <map>
 #include <type_traits>
@@ -445,12 +446,17 @@ cs_status batch_create_ex(cs_batch **out, cs_plan *const *plans, void *const *a,
         int total = 0;
         for (int p = 0; p < 2; ++p) rec[p].resize(rb * count);
         for (int i = 0; i < count && e == cudaSuccess; ++i) {
-            int tiles = 0;
+            int tiles = 0, id = i;  // grids with equal weights share their B matrices
+            for (int j = 0; j < i; ++j)
+                if (std::memcmp(f[j].w, f[i].w, sizeof(cs::Weights)) == 0) {
+                    id = j;
+                    break;
+                }
             e = cs::tc_batch_fill_record(!bt->split, rec[0].data() + rb * i, f[i].view, *f[i].w, f[i].origin,
-                                         f[i].elements, a[i], b[i], total, &tiles);
+                                         f[i].elements, a[i], b[i], total, id, &tiles);
             if (e == cudaSuccess)
                 e = cs::tc_batch_fill_record(!bt->split, rec[1].data() + rb * i, f[i].view, *f[i].w, f[i].origin,
-                                             f[i].elements, b[i], a[i], total, &tiles);
+                                             f[i].elements, b[i], a[i], total, id, &tiles);
             total += tiles;
         }
         for (int p = 0; p < 2 && e == cudaSuccess; ++p) {

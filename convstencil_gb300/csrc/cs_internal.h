@@ -85,11 +85,13 @@ cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long 
 // device record per grid (tc_batch_record_bytes each, 128-byte aligned)
 // holding its tensor map over `in_base`, output, sizes, first tile and
 // weight digits; tiles of a grid are numbered from tile_begin and *tiles
-// returns their count. One launch advances every grid by one sweep.
+// returns their count. Records with the same digits_id must hold the same
+// weights (a CTA crossing between them keeps its B matrices). One launch
+// advances every grid by one sweep; each CTA takes a contiguous run of tiles.
 size_t tc_batch_record_bytes(bool fp64);
 cudaError_t tc_batch_fill_record(bool fp64, void *rec, const GridView &g, const Weights &w, long long origin,
                                  long long elements, const void *in_base, void *out_base, int tile_begin,
-                                 int *tiles);
+                                 int digits_id, int *tiles);
 cudaError_t launch_tc_batch(bool fp64, const void *records, int ngrids, int total_tiles, const TcWait &wait,
                             cudaStream_t stream);
 // 2D tensor map over a whole (hi, lo) buffer of `rows` x `ld` pairs, box_x x box_y tiles.

@@ -289,6 +289,7 @@ struct alignas(128) TcGrid {
     typename F::Out *out;     // interior point (0, 0) of the destination
     long long ld;
     int m, n, tiles_x, tile_begin, map_x, map_y;
+    int digits_id;            // grids with the same id have the same weights
     typename F::Digits digits;
 };
 
@@ -448,15 +449,19 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
                 int g, x0, y0;
                 tile_at(it, g, x0, y0);
                 if (g != g_bmat) {
-                    // New grid: once the MMAs of the previous tile (and so all
-                    // earlier ones) are done reading B, the warp rewrites it.
-                    int ok = 1;
-                    if (lane == 0 && it > 0) ok = wait(bar2(S.acc_full, (it - 1) & 1), ((it - 1) >> 1) & 1);
-                    if (!__shfl_sync(0xffffffffu, ok, 0)) break;
-                    tc_fence_after();
-                    build_bmat<F>(S, grids[g].digits, lane, 32);
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    __syncwarp();
+                    // New grid with other weights: once the MMAs of the
+                    // previous tile (and so all earlier ones) are done reading
+                    // B, the warp rewrites it. Grids that share the weights
+                    // (the same digits_id) keep it.
+                    if (grids[g].digits_id != grids[g_bmat].digits_id) {
+                        int ok = 1;
+                        if (lane == 0 && it > 0) ok = wait(bar2(S.acc_full, (it - 1) & 1), ((it - 1) >> 1) & 1);
+                        if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+                        tc_fence_after();
+                        build_bmat<F>(S, grids[g].digits, lane, 32);
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        __syncwarp();
+                    }
                     g_bmat = g;
                 }
             }
@@ -714,7 +719,7 @@ cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long 
 
 template <class F>
 cudaError_t fill_record(void *rec, const GridView &g, const Weights &w, long long origin, long long elements,
-                        const void *in_base, void *out_base, int tile_begin, int *tiles,
+                        const void *in_base, void *out_base, int tile_begin, int digits_id, int *tiles,
                         typename F::Digits (*slice)(const Weights &))
 {
     TcGrid<F> r;
@@ -731,6 +736,7 @@ cudaError_t fill_record(void *rec, const GridView &g, const Weights &w, long lon
     r.tile_begin = tile_begin;
     r.map_x = (int)(origin % ld);
     r.map_y = (int)(origin / ld);
+    r.digits_id = digits_id;
     r.digits = slice(w);
     *tiles = r.tiles_x * (int)((g.ext[0] + TY - 1) / TY);
     std::memcpy(rec, &r, sizeof r);
@@ -746,10 +752,11 @@ cudaError_t launch_batch(const void *records, int ngrids, int total, const WaitC
     std::memset(&unused, 0, sizeof unused);
     const int grid = std::min(total, device_sm_count());
     note_launch();
-    k2d_tc<F, true><<<grid, kThreads<F>, sizeof(Smem<F>) + 128, st>>>(
-        unused, nullptr, 0, 0, 0, 0, total, 0, 0, typename F::Digits{}, wc,
-        reinterpret_cast<const TcGrid<F> *>(records), ngrids);
-    return cudaGetLastError();
+    // The records were written before the previous kernel of the stream ran,
+    // so the set-up may read them before pdl_wait().
+    return launch_programmatic(k2d_tc<F, true>, grid, kThreads<F>, sizeof(Smem<F>) + 128, st, unused,
+                               static_cast<typename F::Out *>(nullptr), 0, 0, 0LL, 0, total, 0, 0,
+                               typename F::Digits{}, wc, reinterpret_cast<const TcGrid<F> *>(records), ngrids);
 }
 
 split::SliceWeights split_digits(const Weights &w) { return split::slice_weights(w); }
@@ -775,12 +782,12 @@ size_t tc_batch_record_bytes(bool fp64) { return fp64 ? sizeof(TcGrid<FmtF64>) :
 
 cudaError_t tc_batch_fill_record(bool fp64, void *rec, const GridView &g, const Weights &w, long long origin,
                                  long long elements, const void *in_base, void *out_base, int tile_begin,
-                                 int *tiles)
+                                 int digits_id, int *tiles)
 {
-    return fp64 ? fill_record<FmtF64>(rec, g, w, origin, elements, in_base, out_base, tile_begin, tiles,
+    return fp64 ? fill_record<FmtF64>(rec, g, w, origin, elements, in_base, out_base, tile_begin, digits_id, tiles,
                                       f64_slice_weights)
-                : fill_record<FmtSplit>(rec, g, w, origin, elements, in_base, out_base, tile_begin, tiles,
-                                        split_digits);
+                : fill_record<FmtSplit>(rec, g, w, origin, elements, in_base, out_base, tile_begin, digits_id,
+                                        tiles, split_digits);
 }
 
 cudaError_t launch_tc_batch(bool fp64, const void *records, int ngrids, int total_tiles, const TcWait &wt,

@@ -3,7 +3,8 @@
 When a plan's kernel is known without a timing run, cs_run_host moves the
 grid in row bands (slabs of the slowest axis), runs the sweeps as a
 wavefront over the bands while the later bands are still arriving, and copies
-each band back as soon as its last sweep is done. The bands are cut at
+each band back as soon as its last sweep is done (split plans on the tcgen05
+kernel launch whole sets of independent band-sweeps as one batch). The bands are cut at
 multiples of the kernels' tile heights, so every tile sees the same window as
 in a whole-grid sweep: the result must be bitwise the device path's."""
 import numpy as np
@@ -67,6 +68,24 @@ def test_banded_host_run_equals_device_run(shape, ext, prec, algo, steps):
     dp = ctypes.POINTER(ctypes.c_double)
     cs.check(lib.cs_run_host(p._h, ctypes.cast(pin_in.data_ptr(), dp), ctypes.cast(pin_out.data_ptr(), dp), steps))
     np.testing.assert_array_equal(pin_out.numpy(), dev)
+    assert cs.device_wait_timeouts() == 0
+
+
+@pytest.mark.parametrize("steps", [1, 2, 3, 20, 41])
+def test_batched_band_sets_equal_device_run(steps):
+    """Split box2d3r on SPLIT_TC runs its band-sweeps as batched sets (one
+    tcgen05 batch launch per set c = 2s + k, 16 bands here): every sweep
+    count, fewer sweeps than bands included, is bitwise the device path's."""
+    info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME["box2d3r"]]
+    w = O.seeded_weights(info[1], 90 + steps)
+    ext = (4096, 1000)
+    p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    x = O.splitmix_uniform(int(np.prod(ext)), 91).reshape(ext)
+    buf = p.pack(x)
+    for _ in range(2):  # the second call reuses the plan's band records
+        host = p.run_host(buf, steps)
+        np.testing.assert_array_equal(host, _device(p, buf, steps))
     assert cs.device_wait_timeouts() == 0
 
 
