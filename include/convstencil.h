@@ -203,11 +203,12 @@ CS_API cs_status cs_split_to_fp64(const cs_plan *plan, const void *src, double *
  * device grid (converted to (hi, lo) in place for split plans), runs, copies
  * the result (FP64) to host_out. Synchronous. When the kernel is known
  * without a timing run (pinned, or tuned earlier for this kind of plan), the
- * grid has at least two bands of 1024 rows (2D) or 64 planes (3D), and no
- * temporal blocking or re-anchor sweep is involved, the copies overlap the
- * sweeps: the grid moves in bands, the sweeps run as a wavefront over the
- * bands already there, and each band returns after its last sweep (results
- * bitwise those of whole-grid sweeps). The two device grids are
+ * grid has at least two bands (256 rows for split 7x7 plans on the tensor
+ * cores, else 1024 rows in 2D or 64 planes in 3D), and no temporal blocking
+ * or re-anchor sweep is involved, the copies overlap the sweeps: the grid
+ * moves in bands, the sweeps run as a wavefront over the bands already there,
+ * and each band returns after its last sweep (results bitwise those of
+ * whole-grid sweeps). The two device grids are
  * allocated by the plan's first call and kept for its later calls until
  * cs_plan_destroy (a call that finds them in use by another thread allocates
  * and frees its own). Returns CS_ERR_TIMEOUT (result incomplete) if a
