@@ -197,6 +197,12 @@ def kernel_launch_count() -> int:
     return int(lib().cs_kernel_launch_count())
 
 
+def release_cached_plan() -> None:
+    """Frees the plan and device grids the reference-shaped wrappers keep
+    from their latest call (cs_release_cached_plan)."""
+    lib().cs_release_cached_plan()
+
+
 def last_loop_seconds() -> float:
     return float(lib().cs_last_loop_seconds())
 

@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -1279,10 +1280,55 @@ void print_timing(const char *banner, bool secs_line, double secs, double points
     fflush(stdout);
 }
 
-struct PlanGuard {
-    cs_plan *p = nullptr;
-    ~PlanGuard() { cs_plan_destroy(p); }
+// The reference-shaped wrappers keep the plan of their latest call, with the
+// two device grids host_run keeps in it, for the next call with the same
+// shape, layout and weights: repeated calls (a solver's time loop) skip the
+// plan set-up and the grid allocation. A call with other arguments replaces
+// it, cs_release_cached_plan() frees it. The cache is never destroyed by a
+// static destructor (the CUDA runtime may be gone by then); the process exit
+// returns its memory.
+struct RefPlanCache {
+    std::mutex mu;
+    std::shared_ptr<cs_plan> plan;
+    std::vector<long long> key;
 };
+RefPlanCache &ref_cache()
+{
+    static RefPlanCache *c = new RefPlanCache;
+    return *c;
+}
+
+cs_status ref_plan(std::shared_ptr<cs_plan> *out, cs_shape shape, const long long *ext, const double *params,
+                   const cs_layout &L)
+{
+    const int nw = kShapes[shape].n_fused;
+    std::vector<long long> key = {(long long)shape, L.dims, L.halo, L.origin, L.elements};
+    for (int d = 0; d < L.dims; ++d) key.insert(key.end(), {L.extent[d], L.pitch[d]});
+    for (int i = 0; i < nw; ++i) {
+        long long bits;
+        std::memcpy(&bits, &params[i], sizeof bits);
+        key.push_back(bits);
+    }
+    RefPlanCache &c = ref_cache();
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (c.plan && c.key == key) {
+            *out = c.plan;
+            return CS_OK;
+        }
+    }
+    cs_plan *p = nullptr;
+    const cs_status s = make_ref_plan(&p, shape, ext, params, L);
+    if (s != CS_OK) return s;
+    std::shared_ptr<cs_plan> sp(p, cs_plan_destroy);
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        c.plan = sp;
+        c.key = std::move(key);
+    }
+    *out = std::move(sp);
+    return CS_OK;
+}
 
 cs_status check_ref_args(const void *in, const void *out, const void *params, int times,
                          std::initializer_list<int> dims)
@@ -1297,6 +1343,15 @@ cs_status check_ref_args(const void *in, const void *out, const void *params, in
 }  // namespace
 
 extern "C" {
+
+CS_API void cs_release_cached_plan(void)
+{
+    std::shared_ptr<cs_plan> old;
+    RefPlanCache &c = ref_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    old.swap(c.plan);
+    c.key.clear();
+}
 
 CS_API cs_status cs_run_host(cs_plan *p, const double *host_in, double *host_out, long long steps)
 {
@@ -1319,11 +1374,11 @@ CS_API cs_status cs_gpu_1d1r(const double *in, double *out, const double *params
     L.origin = 4;
     L.elements = (long long)n + 7;
     const long long ext[1] = {n};
-    PlanGuard g;
-    s = make_ref_plan(&g.p, CS_SHAPE_1D1R, ext, params, L);
+    std::shared_ptr<cs_plan> g;
+    s = ref_plan(&g, CS_SHAPE_1D1R, ext, params, L);
     if (s != CS_OK) return s;
     double secs = 0;
-    s = host_run(g.p, in, (size_t)n + 7, out, 1, (size_t)n + 6, 3LL * times, &secs);
+    s = host_run(g.get(), in, (size_t)n + 7, out, 1, (size_t)n + 6, 3LL * times, &secs);
     if (s == CS_OK) print_timing("ConvStencil(1D): ", false, secs, (double)n, 3, times);
     return s;
 }
@@ -1343,11 +1398,11 @@ CS_API cs_status cs_gpu_star_1d2r_step2(const double *in, double *out, const dou
     L.origin = 4;
     L.elements = (long long)n + 8;
     const long long ext[1] = {n};
-    PlanGuard g;
-    s = make_ref_plan(&g.p, CS_SHAPE_1D2R, ext, params, L);
+    std::shared_ptr<cs_plan> g;
+    s = ref_plan(&g, CS_SHAPE_1D2R, ext, params, L);
     if (s != CS_OK) return s;
     double secs = 0;
-    s = host_run(g.p, in, (size_t)n + 8, out, 0, (size_t)n + 7, 2LL * times, &secs);
+    s = host_run(g.get(), in, (size_t)n + 8, out, 0, (size_t)n + 7, 2LL * times, &secs);
     if (s == CS_OK) print_timing(nullptr, false, secs, (double)n, 2, times);
     return s;
 }
@@ -1368,12 +1423,12 @@ static cs_status gpu_2d(cs_shape shape, const double *in, double *out, const dou
     L.origin = 3 * L.pitch[0] + 4;
     L.elements = ((long long)m + 6) * L.pitch[0];
     const long long ext[2] = {m, n};
-    PlanGuard g;
-    s = make_ref_plan(&g.p, shape, ext, params, L);
+    std::shared_ptr<cs_plan> g;
+    s = ref_plan(&g, shape, ext, params, L);
     if (s != CS_OK) return s;
     double secs = 0;
     const size_t all = (size_t)L.elements;
-    s = host_run(g.p, in, all, out, 0, all, (long long)steps_mult * times, &secs);
+    s = host_run(g.get(), in, all, out, 0, all, (long long)steps_mult * times, &secs);
     if (s == CS_OK) print_timing("ConvStencil(2D): ", false, secs, (double)m * n, steps_mult, times);
     return s;
 }
@@ -1410,12 +1465,12 @@ static cs_status gpu_3d(cs_shape shape, const double *in, double *out, const dou
     L.origin = 3 * L.pitch[0] + 3 * L.pitch[1] + 3;
     L.elements = ((long long)h + 6) * L.pitch[0];
     const long long ext[3] = {h, m, n};
-    PlanGuard g;
-    s = make_ref_plan(&g.p, shape, ext, params, L);
+    std::shared_ptr<cs_plan> g;
+    s = ref_plan(&g, shape, ext, params, L);
     if (s != CS_OK) return s;
     double secs = 0;
     const size_t all = (size_t)L.elements;
-    s = host_run(g.p, in, all, out, 0, all, 3LL * times, &secs);
+    s = host_run(g.get(), in, all, out, 0, all, 3LL * times, &secs);
     if (s == CS_OK) print_timing(banner, true, secs, (double)h * m * n, 3, times);
     return s;
 }

@@ -219,7 +219,11 @@ CS_API cs_status cs_run_host(cs_plan *plan, const double *host_in, double *host_
 /* ---- reference-shaped wrappers (FUSED semantics, reference layouts) ---- */
 /* Each returns CS_ERR_TIMEOUT (result incomplete) if a bounded device-side
  * wait expired during the call; the reference exits on any CUDA error
- * (src/2d/2d_utils.h:35-65). */
+ * (src/2d/2d_utils.h:35-65). Unlike the reference, which allocates and frees
+ * its device arrays on every call, the wrappers keep the plan of their latest
+ * call and its two device grids for the next call with the same shape, sizes
+ * and params (a time loop then skips the set-up and the allocation); a call
+ * with other arguments replaces it and cs_release_cached_plan() frees it. */
 /* Replaces gpu_1d1r (src/1d/1d_utils.h:75, src/1d/gpu_1r.cu:227-302).
  * in: n+7 doubles (index 0 alignment pad, halo 3); out: n+6 doubles, the
  * device array from index 1 (src/1d/gpu_1r.cu:299). params: 7. */
@@ -326,6 +330,10 @@ CS_API void cs_set_verbose(int on);
 /* Seconds of GPU time of the last timed loop run by a reference-shaped
  * wrapper on this thread (CUDA events around the launch loop). */
 CS_API double cs_last_loop_seconds(void);
+/* Frees the plan and device grids the reference-shaped wrappers keep from
+ * their latest call (no counterpart in the reference, whose wrappers keep
+ * nothing). Safe to call at any time; the next wrapper call builds anew. */
+CS_API void cs_release_cached_plan(void);
 /* Number of kernel launches issued by this process so far. */
 CS_API long long cs_kernel_launch_count(void);
 /* Library version string. */

@@ -102,3 +102,30 @@ def test_banded_reference_wrapper_matches_oracle():
         out = np.zeros_like(g).reshape(-1)
         cs.gpu_box_2d3r(g.reshape(-1).copy(), out, w, 4, m, n)
         assert rel_err(out, ref)[0] <= 1e-12
+
+
+def test_reference_wrapper_keeps_its_latest_plan():
+    """cs_gpu_box_2d3r keeps the plan (and device grids) of its latest call
+    for the next call with the same arguments; other sizes or weights replace
+    it and cs_release_cached_plan frees it. Every call's result is the
+    oracle's, whichever way the plan was obtained."""
+    def call(m, n, wseed, steps):
+        w = O.seeded_weights(49, wseed)
+        x = O.splitmix_uniform(m * n, wseed + 1).reshape(m, n)
+        g = np.zeros((m + 6, n + 8))
+        g[3:m + 3, 4:n + 4] = x
+        out = np.zeros_like(g).reshape(-1)
+        cs.gpu_box_2d3r(g.reshape(-1).copy(), out, w, steps, m, n)
+        ref = O.run_2d(g, w, 3, m, n, 3, 4, steps).reshape(-1)
+        assert rel_err(out, ref)[0] <= 1e-12
+        return out
+    a1 = call(1536, 1200, 80, 3)
+    a2 = call(1536, 1200, 80, 3)   # same arguments: the kept plan
+    np.testing.assert_array_equal(a1, a2)
+    call(1536, 1200, 82, 3)        # other weights: a new plan
+    call(640, 520, 80, 2)          # other sizes: a new plan
+    cs.release_cached_plan()
+    a3 = call(1536, 1200, 80, 3)   # after the release: built anew
+    np.testing.assert_array_equal(a1, a3)
+    cs.release_cached_plan()
+    assert cs.device_wait_timeouts() == 0
