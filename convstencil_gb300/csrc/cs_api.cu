@@ -296,6 +296,14 @@ bool fp64_tc_geometry_ok(const cs_plan *p)
 
 bool fp64_tc_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc_geometry_ok(p); }
 
+// FP64 plans of dense 3x3x3 stencils run on the 3D tcgen05 digit pipeline
+// (the same work items as the split 3D kernel, six digits per point).
+bool fp64_tc3d_geometry_ok(const cs_plan *p)
+{
+    return p->dims == 3 && p->radius == 1 && p->pattern == cs::PAT_DENSE;
+}
+bool fp64_tc3d_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc3d_geometry_ok(p); }
+
 // Split plans of 3D radius-1 stencils (27 weights) also run on the tcgen05
 // slice kernel.
 bool split_tc3d_ok(const cs_plan *p)
@@ -318,6 +326,9 @@ cudaError_t launch_sweep_rows(const cs_plan *p, int algo, const void *in_base, v
         const double *in = (const double *)in_base + off;
         double *out = (double *)out_base + off;
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(v, p->w, in, out, st);
+        if (algo == CS_ALGO_FP64_TC && fp64_tc3d_ok(p) && cs::split_tc3d_layout_ok(v, off, in_base, out_base))
+            return cs::launch_fp64_sweep_tc3d(v, p->w, off, p->layout.elements, (const double *)in_base,
+                                              (double *)out_base, p->wait, st);
         if (algo == CS_ALGO_FP64_TC && fp64_tc_ok(p) && reinterpret_cast<uintptr_t>(out_base) % 16 == 0 &&
             cs::split_tma_layout_ok(v, off, in_base))
             return cs::launch_fp64_sweep_tc(v, p->w, off, p->layout.elements, (const double *)in_base,
@@ -396,17 +407,18 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
         cand[nc++] = CS_ALGO_SPLIT_MMA_TMA;
         cand[nc++] = CS_ALGO_SPLIT_FMA;
     } else {
-        if ((p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) || (p->algo == CS_ALGO_FP64_TC && fp64_tc_ok(p))) {
+        const bool tc = fp64_tc_ok(p) || fp64_tc3d_ok(p);
+        if ((p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) || (p->algo == CS_ALGO_FP64_TC && tc)) {
             *out = p->algo;
             return CS_OK;
         }
-        if (p->algo != CS_ALGO_AUTO || (!fp64_mma_ok(p) && !fp64_tc_ok(p))) {
+        if (p->algo != CS_ALGO_AUTO || (!fp64_mma_ok(p) && !tc)) {
             *out = CS_ALGO_FP64_FMA;
             return CS_OK;
         }
         cand[nc++] = CS_ALGO_FP64_FMA;
         if (fp64_mma_ok(p)) cand[nc++] = CS_ALGO_FP64_MMA;
-        if (fp64_tc_ok(p)) cand[nc++] = CS_ALGO_FP64_TC;
+        if (tc) cand[nc++] = CS_ALGO_FP64_TC;
     }
     auto key = std::make_tuple(p->dims, p->radius, p->pattern, (int)p->prec, size_class(p));
     {
@@ -577,6 +589,8 @@ cudaError_t fp64_anchor_sweep_fp64_in(const cs_plan *p, const void *src, void *d
     const long long n = p->layout.elements, off = p->layout.origin;
     if (fp64_tc_geometry_ok(p) && reinterpret_cast<uintptr_t>(dst) % 16 == 0 && split_tma_layout_ok(p->view, off, src))
         return launch_fp64_sweep_tc(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
+    if (fp64_tc3d_geometry_ok(p) && split_tc3d_layout_ok(p->view, off, src, dst))
+        return launch_fp64_sweep_tc3d(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
     return launch_fp64_fma(p->view, p->radius, p->pattern, p->w, (const double *)src + off, (double *)dst + off, st);
 }
 
@@ -831,9 +845,10 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
         if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
-        if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p))
+        if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p) && !fp64_tc3d_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
-                        "FP64 tcgen05 serves 2D radius-3 FP64 plans of at least 8x8 on even-aligned layouts");
+                        "FP64 tcgen05 serves 2D radius-3 FP64 plans of at least 8x8 on even-aligned layouts "
+                        "and dense 3x3x3 FP64 plans");
         if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
             p->algo = (int)v;
             return CS_OK;

@@ -109,6 +109,13 @@ bool split_tc3d_layout_ok(const GridView &g, long long origin, const void *in_ba
 cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
                                     long long elements, const float2 *in_base, float2 *out_base,
                                     const TcWait &wait, cudaStream_t stream);
+// The same pipeline on FP64 grids of dense 3x3x3 plans: six digits cut from
+// the FP64 bits with integer operations, exact level sums, one rounding to
+// FP64 per output (an output whose parts had different plane exponents is
+// summed in FP64). Same layout conditions.
+cudaError_t launch_fp64_sweep_tc3d(const GridView &g, const Weights &w, long long origin, long long elements,
+                                   const double *in_base, double *out_base, const TcWait &wait,
+                                   cudaStream_t stream);
 int device_sm_count();
 // Bounded device-side waits that expired since the last reset (TMA/mma.sync
 // kernel, 2D and 3D tcgen05 kernels).

@@ -50,9 +50,9 @@
 #include "cs_internal.h"
 #include "cs_split_common.cuh"
 #include "cs_tc_common.cuh"
+#include "cs_tc_f64.cuh"
 
 #include <algorithm>
-#include <mutex>
 
 namespace cs {
 
@@ -61,11 +61,29 @@ __device__ unsigned int g_tc3d_wait_timeouts;
 namespace {
 
 using split::kDigitBits;
-using split::kDigits;
 using split::SliceWeights;
 using split::slice_digits;
 using split::two_sum;
 using namespace tc;
+
+// Number formats: split (FP32 (hi, lo) grids, five digits, a ring of three
+// 160-column TMEM blocks) and FP64 (FP64 grids, six digits cut with integer
+// operations as in the 2D kernel, a ring of two 192-column blocks: three do
+// not fit in the 512 columns).
+struct F3Split {
+    static constexpr bool kF64 = false;
+    static constexpr int D = split::kDigits;  // 5
+    static constexpr int NBLK = 3;
+    using Out = float2;
+    using Digits = SliceWeights;
+};
+struct F3F64 {
+    static constexpr bool kF64 = true;
+    static constexpr int D = 6;
+    static constexpr int NBLK = 2;
+    using Out = double;
+    using Digits = F64Weights;
+};
 
 // Warp roles. Warp w issues from the SM's scheduler w % 4, and an epilogue
 // warp can read only TMEM lanes 32 (w % 4) .. + 31, so each scheduler hosts
@@ -98,13 +116,13 @@ constexpr int PL = ST_X * ST_Y;              // halves per digit plane (2,592 by
 constexpr unsigned kRowBytes = ST_X * 2;     // 144
 constexpr int NOFF = 3;                      // window row offsets
 constexpr int NLV = 32;                      // TMEM columns per level: 4 tap planes (3 + padding) x 8
-constexpr int NCOL = NLV * kDigits;          // 160 columns per input-plane block
-constexpr int NBLK = 3;                      // input-plane blocks in TMEM (ring)
+template <class F>
+constexpr int kNcol = NLV * F::D;            // columns per input-plane block: 160 split, 192 FP64
 constexpr int kTmemCols = 512;
 constexpr int kStages = 2 * kGroups;         // TMA window buffers (two per slicer group)
 constexpr int NPL = 7;                       // digit-plane sets (ring); also keeps one CTA per SM
 constexpr int kScaleRing = 32;               // per-input-plane scale exponents (ring)
-constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 10,368
+constexpr unsigned kStageBytes = ST_X * ST_Y * 8;  // 10,368 (8-byte points)
 // Column pairs of a window row. Only window columns 3..68 meet a nonzero
 // weight (block b reads columns 8b .. 8b+15, taps at k = c+3 .. c+5), so the
 // slicers cut pairs 1..34 (columns 2..69); the digit planes' columns 0, 1, 70
@@ -112,40 +130,46 @@ constexpr unsigned kStageBytes = ST_X * ST_Y * sizeof(float2);  // 10,368
 // zero weights, so they only need to be finite).
 constexpr int PAIRS = ST_X / 2, CUT0 = 1, NCUTX = 34, NCUT = ST_Y * NCUTX;  // 36, 612
 constexpr int PER = (NCUT + kGroupThreads - 1) / kGroupThreads;            // 5
-static_assert(NBLK * NCOL <= kTmemCols, "TMEM blocks exceed the allocation");
+static_assert(F3Split::NBLK * kNcol<F3Split> <= kTmemCols && F3F64::NBLK * kNcol<F3F64> <= kTmemCols,
+              "TMEM blocks exceed the allocation");
 static_assert(kEpiWarps == 8, "two epilogue warps per TMEM lane quarter, four columns each");
 static_assert(kStageBytes % 128 == 0, "TMA destinations stay 128-byte aligned");
 
+template <class F>
 struct Smem {
-    float2 stage[kStages][ST_Y * ST_X];        // TMA destinations
-    __half planes[NPL][kDigits][PL];           // digit planes of input planes (ring)
-    __half bmat[NOFF][NCOL * 16];              // B_i, K-major 8x16-byte core matrices
+    uint4 stage[kStages][ST_Y * PAIRS];        // TMA destinations: pairs of 8-byte points
+    __half planes[NPL][F::D][PL];              // digit planes of input planes (ring)
+    __half bmat[NOFF][kNcol<F> * 16];          // B_i, K-major 8x16-byte core matrices
     unsigned long long stage_full[kStages], stage_empty[kStages];
     unsigned long long planes_full[NPL], planes_empty[NPL];
-    unsigned long long blk_full[NBLK], blk_empty[NBLK];
+    unsigned long long blk_full[F::NBLK], blk_empty[F::NBLK];
     unsigned tmem;                             // TMEM base column
     int abort;                                 // set by the first expired wait
     int wait_ok[kGroups][2];                   // slicer group leaders' wait results
     int scale_exp[kScaleRing];                 // input-plane scale exponents by plane sequence
-    float red[kGroups][kGroupWarps];
+    float red[kGroups][kGroupWarps];           // split: per-warp max |hi|
+    int redi[kGroups][kGroupWarps];            // FP64: per-warp max biased exponent
 };
+static_assert(sizeof(Smem<F3F64>) + 128 <= 232448 && sizeof(Smem<F3Split>) + 128 <= 232448,
+              "shared memory of one CTA must stay within 227 KB");
 
 // The MMAs of one input plane: window row offset I, input digit D. `a`
 // addresses digit 0, row 0 of the plane's digit planes; descriptor
 // addresses advance in 16-byte units.
-template <int I, int D>
+template <class F, int I, int D>
 __device__ __forceinline__ void plane_mma(unsigned d_base, unsigned long long a, unsigned long long b0)
 {
+    constexpr int NCOL = kNcol<F>;
     constexpr unsigned long long a_off = ((unsigned long long)D * PL * 2 + I * kRowBytes) >> 4;
     constexpr unsigned long long b_off = ((unsigned long long)I * NCOL * 16 * 2) >> 4;
     static_assert(((unsigned long long)D * PL * 2 + I * kRowBytes) % 16 == 0 && (NCOL * 16 * 2) % 16 == 0,
                   "descriptor offsets must be 16-byte multiples");
-    mma_f16(d_base + (unsigned)(NLV * D), a + a_off, b0 + b_off, instr_desc(NLV * (kDigits - D)),
+    mma_f16(d_base + (unsigned)(NLV * D), a + a_off, b0 + b_off, instr_desc(NLV * (F::D - D)),
             (I | D) != 0 ? 1u : 0u);
-    if constexpr (D + 1 < kDigits)
-        plane_mma<I, D + 1>(d_base, a, b0);
+    if constexpr (D + 1 < F::D)
+        plane_mma<F, I, D + 1>(d_base, a, b0);
     else if constexpr (I + 1 < NOFF)
-        plane_mma<I + 1, 0>(d_base, a, b0);
+        plane_mma<F, I + 1, 0>(d_base, a, b0);
 }
 
 // Work item `item` of the sweep: output tile column (x0, y0) on planes
@@ -180,7 +204,7 @@ __device__ __forceinline__ void tmem_ld4(unsigned taddr, float (&v)[4])
 
 // Recombines five exact level sums (level L in units of 2^-9L) into a
 // double-float pair.
-__device__ __forceinline__ void recombine(const float (&acc)[kDigits], float &hi, float &lo)
+__device__ __forceinline__ void recombine(const float (&acc)[split::kDigits], float &hi, float &lo)
 {
     float h1, e1, h2, e2;
     two_sum(acc[0], acc[1] * 0x1p-9f, h1, e1);
@@ -189,13 +213,15 @@ __device__ __forceinline__ void recombine(const float (&acc)[kDigits], float &hi
     two_sum(h2, (e1 + e2) + tail, hi, lo);
 }
 
+template <class F>
 __global__ void __launch_bounds__(kThreads, 1)
-    k3d_tc(const __grid_constant__ CUtensorMap tmap, float2 *__restrict__ out, int h, int m, int n,
+    k3d_tc(const __grid_constant__ CUtensorMap tmap, typename F::Out *__restrict__ out, int h, int m, int n,
            long long ldy, long long ldz, int tiles_x, int tiles_y, int zc, int items, int map_x, int map_y,
-           int map_z, SliceWeights sw, WaitCfg wc)
+           int map_z, typename F::Digits sw, WaitCfg wc)
 {
+    constexpr int D = F::D, NBLK = F::NBLK, NCOL = kNcol<F>;
     extern __shared__ unsigned char smem_raw[];
-    Smem &S = *reinterpret_cast<Smem *>(
+    Smem<F> &S = *reinterpret_cast<Smem<F> *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     pdl_allow_dependents();
@@ -240,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const __half v = (dz < 3 && tj >= 0 && tj < 3) ? sw.d[e][(dz * 3 + i) * 3 + tj] : __float2half(0.f);
         S.bmat[i][(nn >> 3) * 128 + (nn & 7) * 8 + (k >> 3) * 64 + (k & 7)] = v;
     }
-    for (int i = tid; i < NPL * kDigits * PL / 2; i += kThreads)
+    for (int i = tid; i < NPL * D * PL / 2; i += kThreads)
         reinterpret_cast<unsigned *>(&S.planes[0][0][0])[i] = 0u;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
@@ -270,7 +296,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (warp == kWarpMma) {
         // ------------------------------------------------ MMA issuer
         const unsigned long long a_desc0 = smem_desc(smem_addr(S.planes[0][0]), 16, kRowBytes);
-        constexpr unsigned long long kSetUnits = (unsigned long long)kDigits * PL * 2 / 16;
+        constexpr unsigned long long kSetUnits = (unsigned long long)D * PL * 2 / 16;
         const unsigned long long b_desc0 = smem_desc(smem_addr(S.bmat[0]), 128, 256);
         if (lane == 0) {
             int q = 0;
@@ -283,7 +309,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                wait(bar(S.blk_empty, blk), ((q / NBLK) & 1) ^ 1)))
                         break;
                     tc_fence_after();
-                    plane_mma<0, 0>(tmem + (unsigned)(NCOL * blk), a_desc0 + kSetUnits * slot, b_desc0);
+                    plane_mma<F, 0, 0>(tmem + (unsigned)(NCOL * blk), a_desc0 + kSetUnits * slot, b_desc0);
                     mma_commit(bar(S.blk_full, blk));       // block ready for the epilogue
                     mma_commit(bar(S.planes_empty, slot));  // digit planes may be overwritten
                     committed = q + 1;
@@ -314,50 +340,88 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 // (b) window -> registers, then release the stage to the next load.
-                const float4 *stg = reinterpret_cast<const float4 *>(S.stage[sb]);
-                float4 v[PER];
-                float vmax = 0.f;
+                const uint4 *stg = S.stage[sb];
+                uint4 v[PER];
+                float vmax = 0.f;   // split: largest |hi|
+                unsigned emax = 0;  // FP64: largest biased exponent
 #pragma unroll
                 for (int k = 0; k < PER; ++k) {
                     const int u = st + k * kGroupThreads;
-                    v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    v[k] = make_uint4(0u, 0u, 0u, 0u);
                     if (u < NCUT) {
                         v[k] = stg[(u / NCUTX) * PAIRS + CUT0 + u % NCUTX];
-                        vmax = fmaxf(vmax, fmaxf(fabsf(v[k].x), fabsf(v[k].z)));
+                        if constexpr (F::kF64)
+                            emax = max(emax, max((v[k].y >> 20) & 0x7FFu, (v[k].w >> 20) & 0x7FFu));
+                        else
+                            vmax = fmaxf(vmax, fmaxf(fabsf(__uint_as_float(v[k].x)), fabsf(__uint_as_float(v[k].z))));
                     }
                 }
+                if constexpr (F::kF64) {
+                    emax = __reduce_max_sync(0xffffffffu, emax);
+                } else {
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+                    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+                }
                 __syncwarp();
                 if (lane == 0) {
-                    S.red[grp][gw] = vmax;
+                    if constexpr (F::kF64)
+                        S.redi[grp][gw] = (int)emax;
+                    else
+                        S.red[grp][gw] = vmax;
                     mbar_arrive(bar(S.stage_empty, sb));
                 }
                 // (c) digit-plane set free (the MMAs that read it are done)?
                 if (leader) S.wait_ok[grp][1] = wait(bar(S.planes_empty, slot), ((q / NPL) & 1) ^ 1);
                 asm volatile("bar.sync %0, %1;" ::"r"(kSliceBarrier + grp), "n"(kGroupThreads) : "memory");
                 go = S.wait_ok[grp][1];
-                vmax = S.red[grp][0];
+                int ex;
+                if constexpr (F::kF64) {
+                    int eb = S.redi[grp][0];
 #pragma unroll
-                for (int i = 1; i < kGroupWarps; ++i) vmax = fmaxf(vmax, S.red[grp][i]);
-                // (d) every slicer of the group has read wait_ok and red before they are reused
+                    for (int i = 1; i < kGroupWarps; ++i) eb = max(eb, S.redi[grp][i]);
+                    ex = max(eb, 1);
+                } else {
+                    vmax = S.red[grp][0];
+#pragma unroll
+                    for (int i = 1; i < kGroupWarps; ++i) vmax = fmaxf(vmax, S.red[grp][i]);
+                    ex = split::tile_exponent(vmax);
+                }
+                // (d) every slicer of the group has read wait_ok and the maxima before they are reused
                 asm volatile("bar.sync %0, %1;" ::"r"(kSliceBarrier + grp), "n"(kGroupThreads) : "memory");
                 if (!go) break;
-                const int ex = split::tile_exponent(vmax);
-                if (leader) S.scale_exp[q % kScaleRing] = ex;
-                const float to_digits = ldexpf(1.0f, kDigitBits - ex);
+                if (leader) S.scale_exp[q % kScaleRing] = (F::kF64 && ex == 2047) ? kNonFiniteTile : ex;
+                unsigned *dst0 = reinterpret_cast<unsigned *>(&S.planes[slot][0][0]);
+                if constexpr (F::kF64) {
 #pragma unroll
-                for (int k = 0; k < PER; ++k) {
-                    const int u = st + k * kGroupThreads;
-                    if (u < NCUT) {
-                        const int idx = (u / NCUTX) * PAIRS + CUT0 + u % NCUTX;
-                        float d0[kDigits], d1[kDigits];
-                        slice_digits(v[k].x * to_digits, v[k].y * to_digits, d0);
-                        slice_digits(v[k].z * to_digits, v[k].w * to_digits, d1);
-                        unsigned *dst = reinterpret_cast<unsigned *>(&S.planes[slot][0][0]) + idx;
+                    for (int k = 0; k < PER; ++k) {
+                        const int u = st + k * kGroupThreads;
+                        if (u < NCUT) {
+                            const int idx = (u / NCUTX) * PAIRS + CUT0 + u % NCUTX;
+                            const unsigned long long ya = f64_biased_fixed(v[k].x, v[k].y, ex);
+                            const unsigned long long yb = f64_biased_fixed(v[k].z, v[k].w, ex);
+                            unsigned *dst = dst0 + idx;
+                            dst[0 * (PL / 2)] = f64_digit_pair<0>(ya, yb);
+                            dst[1 * (PL / 2)] = f64_digit_pair<1>(ya, yb);
+                            dst[2 * (PL / 2)] = f64_digit_pair<2>(ya, yb);
+                            dst[3 * (PL / 2)] = f64_digit_pair<3>(ya, yb);
+                            dst[4 * (PL / 2)] = f64_digit_pair<4>(ya, yb);
+                            dst[5 * (PL / 2)] = f64_digit_pair<5>(ya, yb);
+                        }
+                    }
+                } else {
+                    const float to_digits = ldexpf(1.0f, kDigitBits - ex);
 #pragma unroll
-                        for (int dg = 0; dg < kDigits; ++dg)
-                            dst[dg * (PL / 2)] = split::pack_h2(d0[dg], d1[dg]);
+                    for (int k = 0; k < PER; ++k) {
+                        const int u = st + k * kGroupThreads;
+                        if (u < NCUT) {
+                            const int idx = (u / NCUTX) * PAIRS + CUT0 + u % NCUTX;
+                            float d0[D], d1[D];
+                            slice_digits(__uint_as_float(v[k].x) * to_digits, __uint_as_float(v[k].y) * to_digits, d0);
+                            slice_digits(__uint_as_float(v[k].z) * to_digits, __uint_as_float(v[k].w) * to_digits, d1);
+                            unsigned *dst = dst0 + idx;
+#pragma unroll
+                            for (int dg = 0; dg < D; ++dg) dst[dg * (PL / 2)] = split::pack_h2(d0[dg], d1[dg]);
+                        }
                     }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -380,6 +444,109 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int mrow = 32 * quarter + lane;
         const int er = mrow >> 3, eb = mrow & 7;
         const unsigned lane_bits = (unsigned)(32 * quarter) << 16;
+        if constexpr (F::kF64) {
+        int q0 = 0;  // first input plane of the item
+        bool ok = true;
+        for (int item = first; item < items && ok; item += step) {
+            const Item wi = item_of(item, tiles_x, tiles_y, zc, h);
+            const int xb = wi.x0 + 8 * eb + 4 * hh, yy = wi.y0 + er;
+            // Running sums of outputs p - 2 (a) and p - 1 (b). A part's six
+            // level sums combine into one 64-bit integer T (value T 2^c,
+            // c = plane exponent + ew - 1080, as in the 2D kernel); while every
+            // part of a sum had the same plane exponent (ea, eb2) the sum stays
+            // an exact integer (27 taps: |T| < 2^63), rounded once at the end.
+            // A part with another exponent turns the sum into an FP64 value
+            // (fa, fb: the bits live in the same words); a part from a window
+            // with an Inf or NaN makes the output NaN (na, nb).
+            long long a[4], b[4];
+            int ea = 0, eb2 = 0;
+            bool fa = false, fb = false, na = false, nb = false;
+            const int ew = sw.ew;
+            auto part_t = [](const float (&acc)[D][4], long long (&t)[4]) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const float lv[6] = {acc[0][c], acc[1][c], acc[2][c], acc[3][c], acc[4][c], acc[5][c]};
+                    t[c] = f64_combine(lv);
+                }
+            };
+            auto add_part = [&](long long (&sm)[4], int &se, bool &fl, bool &nf, const float (&acc)[D][4],
+                                int ex) {
+                if (nf) return;
+                if (ex == kNonFiniteTile) {
+                    nf = true;
+                    return;
+                }
+                long long t[4];
+                part_t(acc, t);
+                if (!fl && ex == se) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) sm[c] += t[c];
+                    return;
+                }
+                if (!fl) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) sm[c] = __double_as_longlong(f64_from_fixed(sm[c], se + ew - 1080));
+                    fl = true;
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    sm[c] = __double_as_longlong(__longlong_as_double(sm[c]) + f64_from_fixed(t[c], ex + ew - 1080));
+            };
+            auto load_part = [&](int q, int dz, float (&acc)[D][4]) {
+                const unsigned col = (unsigned)(NCOL * (q % NBLK) + 8 * dz + 4 * hh);
+#pragma unroll
+                for (int L = 0; L < D; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
+                tmem_wait_ld();
+            };
+            for (int p = 0; p < wi.zn + 2; ++p) {
+                const int q = q0 + p;
+                if (!(ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1))) break;
+                tc_fence_after();
+                const int ex = S.scale_exp[q % kScaleRing];
+                float acc[D][4];
+                // z tap 2 of output p - 2: its last part; store.
+                load_part(q, 2, acc);
+                if (p >= 2) {
+                    add_part(a, ea, fa, na, acc, ex);
+                    if (yy < m) {
+                        double res[4];
+#pragma unroll
+                        for (int c = 0; c < 4; ++c)
+                            res[c] = na ? __longlong_as_double(0x7FF8000000000000ll)
+                                 : fa ? __longlong_as_double(a[c])
+                                      : f64_from_fixed(a[c], ea + ew - 1080);
+                        double *op = out + (long long)(wi.zs + p - 2) * ldz + (long long)yy * ldy + xb;
+#pragma unroll
+                        for (int c = 0; c < 4; c += 2) {
+                            if (xb + c + 1 < n)
+                                *reinterpret_cast<double2 *>(op + c) = make_double2(res[c], res[c + 1]);
+                            else if (xb + c < n)
+                                op[c] = res[c];
+                        }
+                    }
+                }
+                // z tap 1 of output p - 1.
+                load_part(q, 1, acc);
+                if (p >= 1 && p - 1 < wi.zn) add_part(b, eb2, fb, nb, acc, ex);
+                // z tap 0 of output p: its first part. The block is then
+                // drained and handed back.
+                load_part(q, 0, acc);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(S.blk_empty, q % NBLK));
+#pragma unroll
+                for (int c = 0; c < 4; ++c) a[c] = b[c];  // rotate: p - 1 becomes p - 2, p starts
+                ea = eb2;
+                fa = fb;
+                na = nb;
+                eb2 = ex;
+                fb = false;
+                nb = ex == kNonFiniteTile;
+                if (!nb) part_t(acc, b);
+            }
+            q0 += wi.zn + 2;
+        }
+        } else {
         int q0 = 0;  // first input plane of the item
         bool ok = true;
         for (int item = first; item < items && ok; item += step) {
@@ -413,7 +580,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             };
             // Adds a tap plane's part (five levels per column, relative to
             // 2^ex) to a running sum.
-            auto add_part = [&](float (&sm)[4][4], int &se, bool &fl, const float (&acc)[kDigits][4], int ex) {
+            auto add_part = [&](float (&sm)[4][4], int &se, bool &fl, const float (&acc)[D][4], int ex) {
                 if (!fl && ex == se) {
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
@@ -435,19 +602,19 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    float lv[kDigits], ph, pl, s2, e2;
+                    float lv[D], ph, pl, s2, e2;
 #pragma unroll
-                    for (int L = 0; L < kDigits; ++L) lv[L] = acc[L][c];
+                    for (int L = 0; L < D; ++L) lv[L] = acc[L][c];
                     recombine(lv, ph, pl);
                     two_sum(sm[0][c] * ra, ph * rb, s2, e2);
                     sm[1][c] = sm[1][c] * ra + (e2 + pl * rb);
                     sm[0][c] = s2;
                 }
             };
-            auto load_part = [&](int q, int dz, float (&acc)[kDigits][4]) {
+            auto load_part = [&](int q, int dz, float (&acc)[D][4]) {
                 const unsigned col = (unsigned)(NCOL * (q % NBLK) + 8 * dz + 4 * hh);
 #pragma unroll
-                for (int L = 0; L < kDigits; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
+                for (int L = 0; L < D; ++L) tmem_ld4(tmem + lane_bits + col + NLV * L, acc[L]);
                 tmem_wait_ld();
             };
             for (int p = 0; p < wi.zn + 2; ++p) {
@@ -455,7 +622,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (!(ok = wait(bar(S.blk_full, q % NBLK), (q / NBLK) & 1))) break;
                 tc_fence_after();
                 const int ex = S.scale_exp[q % kScaleRing];
-                float acc[kDigits][4];
+                float acc[D][4];
                 // z tap 2 of output p - 2: its last part; store.
                 load_part(q, 2, acc);
                 if (p >= 2) {
@@ -506,6 +673,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             q0 += wi.zn + 2;
         }
+        }
     }
 
     // Exit: every role is done or has given up. Let the last window loads and
@@ -535,20 +703,21 @@ bool split_tc3d_layout_ok(const GridView &g, long long origin, const void *in_ba
            reinterpret_cast<uintptr_t>(in_base) % 16 == 0 && reinterpret_cast<uintptr_t>(out_base) % 16 == 0;
 }
 
-cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
-                                    long long elements, const float2 *in_base, float2 *out_base,
-                                    const TcWait &wt, cudaStream_t st)
+namespace {
+
+template <class F>
+cudaError_t launch_tc3d(const GridView &g, const typename F::Digits &digits, long long origin, long long elements,
+                        const void *in_base, void *out_base, const TcWait &wt, cudaStream_t st)
 {
     const long long ldy = g.pitch[1], ldz = g.pitch[0];
     CUtensorMap map;
-    cudaError_t e = encode_split_window_map_3d(&map, in_base, ldy, ldz, elements / ldz, ST_X, ST_Y);
+    // The map copies 8-byte points whatever they hold ((hi, lo) pairs or FP64).
+    cudaError_t e = encode_split_window_map_3d(&map, reinterpret_cast<const float2 *>(in_base), ldy, ldz,
+                                               elements / ldz, ST_X, ST_Y);
     if (e != cudaSuccess) return e;
-    const size_t smem = sizeof(Smem) + 128;
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, [smem] {
-        attr_err = cudaFuncSetAttribute(k3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    });
+    const size_t smem = sizeof(Smem<F>) + 128;
+    static const cudaError_t attr_err =
+        cudaFuncSetAttribute(k3d_tc<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr_err != cudaSuccess) return attr_err;
     const int h = (int)g.ext[0], m = (int)g.ext[1], n = (int)g.ext[2];
     const int tiles_x = (n + TX - 1) / TX, tiles_y = (m + TY - 1) / TY;
@@ -567,9 +736,25 @@ cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long lo
     const int items = (int)(txy * ((h + zc - 1) / zc));
     const int grid = std::min(items, sms);
     note_launch();
-    return launch_programmatic(k3d_tc, grid, kThreads, smem, st, map, out_base + origin, h, m, n, ldy, ldz, tiles_x,
+    return launch_programmatic(k3d_tc<F>, grid, kThreads, smem, st, map,
+                               reinterpret_cast<typename F::Out *>(out_base) + origin, h, m, n, ldy, ldz, tiles_x,
                                tiles_y, zc, items, (int)(origin % ldy), (int)((origin % ldz) / ldy),
-                               (int)(origin / ldz), split::slice_weights(w, 27), WaitCfg{wt.limit_ns, wt.skip_loads});
+                               (int)(origin / ldz), digits, WaitCfg{wt.limit_ns, wt.skip_loads});
+}
+
+}  // namespace
+
+cudaError_t launch_split_sweep_tc3d(const GridView &g, const Weights &w, long long origin,
+                                    long long elements, const float2 *in_base, float2 *out_base,
+                                    const TcWait &wt, cudaStream_t st)
+{
+    return launch_tc3d<F3Split>(g, split::slice_weights(w, 27), origin, elements, in_base, out_base, wt, st);
+}
+
+cudaError_t launch_fp64_sweep_tc3d(const GridView &g, const Weights &w, long long origin, long long elements,
+                                   const double *in_base, double *out_base, const TcWait &wt, cudaStream_t st)
+{
+    return launch_tc3d<F3F64>(g, f64_slice_weights(w, 27), origin, elements, in_base, out_base, wt, st);
 }
 
 cudaError_t split_tc3d_wait_timeouts(unsigned *count, bool reset)
