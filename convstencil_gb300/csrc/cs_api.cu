@@ -296,12 +296,12 @@ bool fp64_tc_geometry_ok(const cs_plan *p)
 
 bool fp64_tc_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc_geometry_ok(p); }
 
-// FP64 plans of dense 3x3x3 stencils run on the 3D tcgen05 digit pipeline
-// (the same work items as the split 3D kernel, six digits per point).
-bool fp64_tc3d_geometry_ok(const cs_plan *p)
-{
-    return p->dims == 3 && p->radius == 1 && p->pattern == cs::PAT_DENSE;
-}
+// FP64 plans of 3D radius-1 stencils run on the 3D tcgen05 digit pipeline
+// (the same work items as the split 3D kernel, six digits per point). The
+// plan holds the 3x3x3 weights with zeros outside its pattern, and the
+// pipeline's cost does not depend on how many taps are nonzero, so the
+// 7-point star takes it too.
+bool fp64_tc3d_geometry_ok(const cs_plan *p) { return p->dims == 3 && p->radius == 1; }
 bool fp64_tc3d_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc3d_geometry_ok(p); }
 
 // Split plans of 3D radius-1 stencils (27 weights) also run on the tcgen05
@@ -848,7 +848,7 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
         if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p) && !fp64_tc3d_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
                         "FP64 tcgen05 serves 2D radius-3 FP64 plans of at least 8x8 on even-aligned layouts "
-                        "and dense 3x3x3 FP64 plans");
+                        "and 3D radius-1 FP64 plans");
         if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
             p->algo = (int)v;
             return CS_OK;

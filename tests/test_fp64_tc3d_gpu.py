@@ -1,5 +1,5 @@
-"""FP64 dense 3x3x3 plans on the 3D tcgen05 digit pipeline (CS_ALGO_FP64_TC),
-through the C ABI.
+"""FP64 3D radius-1 plans (the dense 3x3x3 box and the 7-point star) on the
+3D tcgen05 digit pipeline (CS_ALGO_FP64_TC), through the C ABI.
 
 The 3D sweep reads FP64 grids, cuts every input plane of a 16 x 64 tile
 column into six exact 9-bit digits relative to the plane's largest exponent
@@ -133,7 +133,22 @@ def test_fp64_tc3d_tuner_picks_it():
     assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
 
 
+@pytest.mark.parametrize("ext,steps", [((20, 36, 70), 3), ((64, 64, 64), 2)])
+def test_fp64_tc3d_star(ext, steps):
+    """The 7-point star: its 3x3x3 weights with zeros outside the star."""
+    w7 = O.seeded_weights(7, 72 + steps)
+    p = cs.Plan("star3d1r", ext, w7)
+    p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    x = O.splitmix_uniform(int(np.prod(ext)), 73).reshape(ext)
+    buf = p.pack(x)
+    got = dev_run(p, buf, steps)
+    assert p.algo == cs.Algo.FP64_TC
+    ref = oracle_3d(p, buf, O.star3d1r_to_dense(w7), steps)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
 def test_fp64_tc3d_refuses_other_3d_plans():
-    p = cs.Plan("star3d1r", (16, 16, 16), O.seeded_weights(7, 1))
+    """Radius-3 3D plans (the reference's fused forms) keep the FP64 FMA kernel."""
+    p = cs.Plan("box3d1r", (16, 16, 16), O.seeded_weights(196, 1), semantics=cs.Semantics.FUSED)
     with pytest.raises(cs.ConvStencilError):
         p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
