@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     const float lv[6] = {acc[0][c], acc[1][c], acc[2][c], acc[3][c], acc[4][c], acc[5][c]};
-                    t[c] = f64_combine(lv);
+                    t[c] = f64_combine_small(lv);  // one z tap: every level below 2^22
                 }
             };
             auto add_part = [&](long long (&sm)[4], int &se, bool &fl, bool &nf, const float (&acc)[D][4],
