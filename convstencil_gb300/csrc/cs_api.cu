@@ -223,6 +223,7 @@ struct cs_plan {
     cs_precision prec;
     int dims, radius, pattern, steps_per_sweep;
     Weights w;
+    Weights w7;  // 2D plans: w at the centre of a 7x7 (the 2D tcgen05 kernels' tap window)
     cs_layout layout;
     GridView view;
     int algo = CS_ALGO_AUTO;
@@ -285,13 +286,27 @@ bool split_mma_ok(const cs_plan *p)
            cs::split_mma_layout_ok(p->view, p->layout.origin);
 }
 
-// FP64 plans of 2D radius-3 stencils (any 7x7 weights) also run on the
-// tcgen05 digit pipeline; like the split slice kernels its error is relative
-// to the tile's scale, so grids smaller than the 8x8 window stay on FP64 FMA.
+// FP64 plans of 2D stencils of radius up to 3 (their weights at the centre of
+// the 7x7, w7) also run on the tcgen05 digit pipeline; like the split slice
+// kernels its error is relative to the tile's scale, so grids smaller than
+// the 8x8 window stay on FP64 FMA.
 bool fp64_tc_geometry_ok(const cs_plan *p)
 {
-    return p->dims == 2 && p->radius == 3 && p->view.ext[0] >= 8 && p->view.ext[1] >= 8 &&
+    return p->dims == 2 && p->radius <= 3 && p->view.ext[0] >= 8 && p->view.ext[1] >= 8 &&
            cs::split_mma_layout_ok(p->view, p->layout.origin);
+}
+
+// Buffers and layout the 2D FP64 tcgen05 sweep can read by TMA: even pitch
+// and interior column (the window's first column, 4 to the left of a tile,
+// must be 16-byte aligned), 16-byte aligned bases. Window rows and columns
+// outside the buffer (a halo narrower than 3 rows or 4 columns) are read as
+// zero by the TMA unit; those inside it but outside the plan's own halo meet
+// zero weights of the 7x7.
+bool fp64_tc_window_ok(const GridView &v, long long off, const void *in_base, const void *out_base)
+{
+    const long long ld = v.pitch[0];
+    return v.dims == 2 && ld % 2 == 0 && (off % ld) % 2 == 0 && reinterpret_cast<uintptr_t>(in_base) % 16 == 0 &&
+           reinterpret_cast<uintptr_t>(out_base) % 16 == 0;
 }
 
 bool fp64_tc_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc_geometry_ok(p); }
@@ -329,9 +344,8 @@ cudaError_t launch_sweep_rows(const cs_plan *p, int algo, const void *in_base, v
         if (algo == CS_ALGO_FP64_TC && fp64_tc3d_ok(p) && cs::split_tc3d_layout_ok(v, off, in_base, out_base))
             return cs::launch_fp64_sweep_tc3d(v, p->w, off, p->layout.elements, (const double *)in_base,
                                               (double *)out_base, p->wait, st);
-        if (algo == CS_ALGO_FP64_TC && fp64_tc_ok(p) && reinterpret_cast<uintptr_t>(out_base) % 16 == 0 &&
-            cs::split_tma_layout_ok(v, off, in_base))
-            return cs::launch_fp64_sweep_tc(v, p->w, off, p->layout.elements, (const double *)in_base,
+        if (algo == CS_ALGO_FP64_TC && fp64_tc_ok(p) && fp64_tc_window_ok(v, off, in_base, out_base))
+            return cs::launch_fp64_sweep_tc(v, p->w7, off, p->layout.elements, (const double *)in_base,
                                             (double *)out_base, p->wait, st);
         return cs::launch_fp64_fma(v, p->radius, p->pattern, p->w, in, out, st, p->active_rows);
     }
@@ -587,8 +601,8 @@ namespace cs {
 cudaError_t fp64_anchor_sweep_fp64_in(const cs_plan *p, const void *src, void *dst, cudaStream_t st)
 {
     const long long n = p->layout.elements, off = p->layout.origin;
-    if (fp64_tc_geometry_ok(p) && reinterpret_cast<uintptr_t>(dst) % 16 == 0 && split_tma_layout_ok(p->view, off, src))
-        return launch_fp64_sweep_tc(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
+    if (fp64_tc_geometry_ok(p) && fp64_tc_window_ok(p->view, off, src, dst))
+        return launch_fp64_sweep_tc(p->view, p->w7, off, n, (const double *)src, (double *)dst, p->wait, st);
     if (fp64_tc3d_geometry_ok(p) && split_tc3d_layout_ok(p->view, off, src, dst))
         return launch_fp64_sweep_tc3d(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
     return launch_fp64_fma(p->view, p->radius, p->pattern, p->w, (const double *)src + off, (double *)dst + off, st);
@@ -799,6 +813,12 @@ CS_API cs_status cs_plan_create(cs_plan **out, cs_shape shape, cs_semantics sem,
     p->steps_per_sweep = sem == CS_SEM_STEP ? 1 : si.fused_steps;
     expand_weights(shape, sem, weights, p->w, p->radius);
     p->pattern = classify(p->w, p->dims, p->radius);
+    memset(p->w7.v, 0, sizeof p->w7.v);
+    if (p->dims == 2 && p->radius <= 3) {
+        const int k = 2 * p->radius + 1, o = 3 - p->radius;
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) p->w7.v[(i + o) * 7 + j + o] = p->w.v[i * k + j];
+    }
     if (layout) {
         const cs_layout &L = *layout;
         bool ok = L.dims == si.dims && L.halo >= p->radius && L.pitch[si.dims - 1] == 1;
@@ -847,8 +867,8 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
         if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p) && !fp64_tc3d_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
-                        "FP64 tcgen05 serves 2D radius-3 FP64 plans of at least 8x8 on even-aligned layouts "
-                        "and 3D radius-1 FP64 plans");
+                        "FP64 tcgen05 serves 2D FP64 plans of radius up to 3 and at least 8x8 on even-aligned "
+                        "layouts and 3D radius-1 FP64 plans");
         if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
             p->algo = (int)v;
             return CS_OK;
@@ -989,7 +1009,7 @@ struct DevBuf {
 // the one-grid kernel, and keep one launch per band-sweep.
 bool band_batch_ok(const cs_plan *p, int algo)
 {
-    return p->prec == CS_PREC_SPLIT && algo == CS_ALGO_SPLIT_TC && fp64_tc_geometry_ok(p);
+    return p->prec == CS_PREC_SPLIT && algo == CS_ALGO_SPLIT_TC && p->radius == 3 && fp64_tc_geometry_ok(p);
 }
 
 bool banded_ok(cs_plan *p, long long sweeps, int *algo, int *bands)

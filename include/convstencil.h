@@ -66,7 +66,7 @@ typedef enum cs_semantics { CS_SEM_STEP = 0, CS_SEM_FUSED = 1 } cs_semantics;
 
 /* Arithmetic of the sweep.
  * CS_PREC_FP64 : FP64 grids. FP64 FMA or FP64 MMA arithmetic, or, for 2D
- *                dense 7x7 and 3D radius-1 kernels, the FP64-accurate
+ *                kernels up to 7x7 and 3D radius-1 kernels, the FP64-accurate
  *                tensor-core form (CS_ALGO_FP64_TC) when the tuner measures
  *                it faster: every
  *                product and level sum is exact, inputs keep 52 bits below
@@ -100,8 +100,9 @@ typedef enum cs_algo {
     CS_ALGO_FP64_TC = 7   /* FP64 plans on the same tcgen05 pipeline: six exact 9-bit digits per
                              operand cut from the FP64 bits by integer operations, exact FP32
                              level sums, integer recombination to FP64 (no FP64 instruction in
-                             the sweep); 2D dense radius-3 FP64 plans of at least 8x8, same
-                             buffer conditions as CS_ALGO_SPLIT_TC; also 3D radius-1 FP64
+                             the sweep); 2D FP64 plans of radius up to 3 (the weights at the
+                             centre of the 7x7) of at least 8x8, even pitch and interior column,
+                             16-byte aligned buffers; also 3D radius-1 FP64
                              plans, box and star (an output's three plane parts are added as exact
                              integers when their plane exponents agree, in FP64 otherwise) */
 } cs_algo;

@@ -177,11 +177,35 @@ def test_fp64_tc_tuner_picks_it_on_large_grids():
     assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
 
 
+@pytest.mark.parametrize("shape,taps,ext,steps", [("box2d1r", 9, (100, 129), 4), ("star2d1r", 5, (200, 77), 5),
+                                                  ("box2d1r", 9, (8, 8), 2), ("star2d1r", 5, (257, 300), 3)])
+def test_fp64_tc_radius_one_plans(shape, taps, ext, steps):
+    """2D radius-1 plans on the 7x7 tcgen05 kernel (their weights at the
+    centre, native layout with a 1-row, 2-column halo: window rows and
+    columns outside the buffer come from the TMA unit as zeros)."""
+    w = O.seeded_weights(taps, 80 + taps)
+    p = cs.Plan(shape, ext, w)
+    p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    x = O.splitmix_uniform(ext[0] * ext[1], 81).reshape(ext)
+    buf = p.pack(x)
+    got = dev_run(p, buf, steps)
+    assert p.algo == cs.Algo.FP64_TC
+    L = p.layout.as_dict()
+    ld = L["pitch"][0]
+    dense = O.star2d1r_to_dense(w) if shape == "star2d1r" else w
+    ref = O.run_2d(buf.reshape(-1, ld), dense, 1, ext[0], ext[1], L["origin"] // ld, L["origin"] % ld,
+                   steps).reshape(-1)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+    halo = np.ones(p.elements, bool)
+    halo[p.interior_index().reshape(-1)] = False
+    assert not got[halo].any(), "halo must stay zero"
+
+
 def test_fp64_tc_unsupported_plans_refuse_the_algorithm():
     with pytest.raises(cs.ConvStencilError) as e:
         tc_plan((4, 100), O.seeded_weights(49, 1))
     assert e.value.status == 2
-    p = cs.Plan("box2d1r", (64, 64), O.seeded_weights(9, 1))
+    p = cs.Plan("1d2r", (4096,), O.seeded_weights(5, 1))
     with pytest.raises(cs.ConvStencilError):
         p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
     ps = cs.Plan("box2d3r", (64, 64), O.seeded_weights(49, 1), precision=cs.Precision.SPLIT)
