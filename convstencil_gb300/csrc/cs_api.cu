@@ -1012,7 +1012,8 @@ bool band_batch_ok(const cs_plan *p, int algo)
     return p->prec == CS_PREC_SPLIT && algo == CS_ALGO_SPLIT_TC && p->radius == 3 && fp64_tc_geometry_ok(p);
 }
 
-bool banded_ok(cs_plan *p, long long sweeps, int *algo, int *bands)
+// `kept`: the run uses the plan's kept grids (batched sets allowed).
+bool banded_ok(cs_plan *p, long long sweeps, bool kept, int *algo, int *bands)
 {
     if (p->dims < 2 || sweeps < 1) return false;
     if (p->prec == CS_PREC_SPLIT && cs::split_tb_supported(p->dims, p->radius, p->pattern) && p->time_block != 1)
@@ -1020,7 +1021,7 @@ bool banded_ok(cs_plan *p, long long sweeps, int *algo, int *bands)
     if (p->prec == CS_PREC_SPLIT && p->reanchor > 0 && sweeps >= p->reanchor) return false;
     if (choose_algo(p, nullptr, nullptr, nullptr, algo, false) != CS_OK || *algo < 0) return false;
     const long long slabs = p->view.ext[0];
-    if (band_batch_ok(p, *algo)) {
+    if (kept && band_batch_ok(p, *algo)) {
         *bands = (int)std::min<long long>(32, slabs / 256);  // one batch launch per set
     } else {
         const long long per = p->dims == 2 ? 1024 : 64;  // slabs per band at least
@@ -1101,8 +1102,12 @@ static cs_status band_table(cs_plan *p, int algo, int bands, long long sweeps, v
     return CS_OK;
 }
 
+// `kept`: d are the plan's kept grids and the caller holds host_mu, so the
+// plan's cached band records (p->band) may be used and rebuilt; a call on
+// grids of its own (another thread holds the kept ones) launches its
+// band-sweeps one by one and leaves the cache alone.
 cs_status host_run_banded(cs_plan *p, int algo, int bands, const double *host_in, double *host_out,
-                          long long sweeps, void *const d[2], double *loop_seconds)
+                          long long sweeps, void *const d[2], bool kept, double *loop_seconds)
 {
     const long long ld0 = p->view.pitch[0];        // elements per slab
     const long long total = p->layout.elements / ld0;  // slabs in the buffer, halo included
@@ -1116,7 +1121,7 @@ cs_status host_run_banded(cs_plan *p, int algo, int bands, const double *host_in
     for (int k = 0; k <= bands; ++k) c[k] = k == 0 ? 0 : k == bands ? total : first + b[k];
     // The tcgen05 batch kernel takes a whole set per launch when every band
     // meets its layout conditions; otherwise each band-sweep is a launch.
-    bool batch = band_batch_ok(p, algo) && reinterpret_cast<uintptr_t>(d[0]) % 16 == 0 &&
+    bool batch = kept && band_batch_ok(p, algo) && reinterpret_cast<uintptr_t>(d[0]) % 16 == 0 &&
                  reinterpret_cast<uintptr_t>(d[1]) % 16 == 0;
     for (int k = 0; k < bands && batch; ++k) {
         GridView v = p->view;
@@ -1256,11 +1261,11 @@ cs_status host_run(cs_plan *p, const double *host_in, size_t in_elems, double *h
     }
     const bool whole = in_elems * elem_bytes == bytes;
     int balgo = 0, bands = 0;
-    if (whole && out_offset == 0 && out_elems == (size_t)n && banded_ok(p, sweeps, &balgo, &bands)) {
+    if (whole && out_offset == 0 && out_elems == (size_t)n && banded_ok(p, sweeps, kept.owns_lock(), &balgo, &bands)) {
         unsigned w0 = 0, w1 = 0;
         s = cs_device_wait_timeouts(&w0, 0);
         if (s != CS_OK) return s;
-        s = host_run_banded(p, balgo, bands, host_in, host_out, sweeps, d, loop_seconds);
+        s = host_run_banded(p, balgo, bands, host_in, host_out, sweeps, d, kept.owns_lock(), loop_seconds);
         if (s != CS_OK) return s;
         p->last_algo = balgo;
         p->last_time_block = 1;

@@ -129,3 +129,35 @@ def test_reference_wrapper_keeps_its_latest_plan():
     np.testing.assert_array_equal(a1, a3)
     cs.release_cached_plan()
     assert cs.device_wait_timeouts() == 0
+
+
+def test_concurrent_host_runs_on_one_plan():
+    """Threads sharing one plan: the call holding the plan's kept grids runs
+    the batched band sets from the plan's cached records, the others run on
+    grids of their own with one launch per band-sweep (and leave the cache
+    alone). Every result is bitwise the device path's."""
+    import threading
+    info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME["box2d3r"]]
+    w = O.seeded_weights(info[1], 95)
+    ext = (4096, 1000)
+    p = cs.Plan("box2d3r", ext, w, precision=cs.Precision.SPLIT)
+    p.set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    x = O.splitmix_uniform(int(np.prod(ext)), 96).reshape(ext)
+    buf = p.pack(x)
+    want = _device(p, buf, 9)
+    out, errs = [None] * 4, []
+
+    def work(i):
+        try:
+            out[i] = p.run_host(buf, 9)
+        except Exception as e:  # reported below
+            errs.append(e)
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errs, errs
+    for o in out:
+        np.testing.assert_array_equal(o, want)
+    assert cs.device_wait_timeouts() == 0
