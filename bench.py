@@ -459,21 +459,21 @@ def run_pipe_peaks():
 
 # ------------------------------------------------------------ ncu cases
 def run_kernel_case(args):
-    """One box2d3r plan (box3d1r on an h x m x n grid for split_tc3d), one
-    algorithm, `sweeps` sweeps on an m x n grid."""
+    """One box2d3r plan (box3d1r on an h x m x n grid for split_tc3d and
+    fp64_tc3d), one algorithm, `sweeps` sweeps on an m x n grid."""
     import torch
     import convstencil_gb300 as cs
     from convstencil_gb300 import workload as WL
     m, n = args.m, args.n
     shape, ext, taps = SHAPE, (m, n), TAPS
-    if args.kernel_case == "split_tc3d":
+    if args.kernel_case in ("split_tc3d", "fp64_tc3d"):
         shape, ext, taps = "box3d1r", (args.h, m, n), 27
     x = WL.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
     w = WL.seeded_weights(taps, WEIGHT_SEED)
     algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA, "fp64_tc": cs.Algo.FP64_TC,
             "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
             "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC,
-            "split_tc3d": cs.Algo.SPLIT_TC}[args.kernel_case]
+            "split_tc3d": cs.Algo.SPLIT_TC, "fp64_tc3d": cs.Algo.FP64_TC}[args.kernel_case]
     split = args.kernel_case.startswith("split")
     p = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
     p.set_option(cs.Option.ALGO, algo)
@@ -587,9 +587,9 @@ def main():
                          "saturated comparison, print their line and exit")
     ap.add_argument("--kernel-case", default=None,
                     choices=["fp64_fma", "fp64_mma", "fp64_tc", "split_mma", "split_mma_tma", "split_fma",
-                             "split_tc", "split_tc3d"],
-                    help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid (split_tc3d: "
-                         "box3d1r on --h x --m x --n) (small cases for ncu captures) and exit")
+                             "split_tc", "split_tc3d", "fp64_tc3d"],
+                    help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid (split_tc3d, "
+                         "fp64_tc3d: box3d1r on --h x --m x --n) (small cases for ncu captures) and exit")
     ap.add_argument("--m", type=int, default=4608)
     ap.add_argument("--n", type=int, default=4608)
     ap.add_argument("--h", type=int, default=256)
