@@ -186,10 +186,13 @@ void native_layout(int dims, int r, const long long *ext, cs_layout &L)
     L.halo = r;
     const long long x0 = round_up(r, 2);  // interior rows start 16-byte aligned
     if (dims == 1) {
+        // at least 4 points of halo on either side: the 1D FP64 tcgen05 sweep
+        // reads rows of the array 4 points wider than their outputs each way
+        const long long h1 = std::max(x0, 4LL);
         L.extent[0] = ext[0];
         L.pitch[0] = 1;
-        L.origin = x0;
-        L.elements = round_up(x0 + ext[0] + r, 2);
+        L.origin = h1;
+        L.elements = round_up(h1 + ext[0] + std::max((long long)r, 4LL), 2);
     } else if (dims == 2) {
         L.extent[0] = ext[0];
         L.extent[1] = ext[1];
@@ -319,6 +322,18 @@ bool fp64_tc_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc_ge
 bool fp64_tc3d_geometry_ok(const cs_plan *p) { return p->dims == 3 && p->radius == 1; }
 bool fp64_tc3d_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc3d_geometry_ok(p); }
 
+// 1D plans of radius up to 3 on the 2D tcgen05 digit kernel through a row
+// view (launch_fp64_sweep_tc_rows1d): rows of 64 outputs, so the interior
+// must be a whole number of rows (at least 8), with an even origin and 4
+// points of halo on either side.
+bool fp64_tc1d_geometry_ok(const cs_plan *p)
+{
+    const long long n = p->view.ext[0], o = p->layout.origin;
+    return p->dims == 1 && p->radius <= 3 && n % 64 == 0 && n >= 512 && o >= 4 && o % 2 == 0 &&
+           p->layout.elements >= o + n + 4;
+}
+bool fp64_tc1d_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc1d_geometry_ok(p); }
+
 // Split plans of 3D radius-1 stencils (27 weights) also run on the tcgen05
 // slice kernel.
 bool split_tc3d_ok(const cs_plan *p)
@@ -341,6 +356,10 @@ cudaError_t launch_sweep_rows(const cs_plan *p, int algo, const void *in_base, v
         const double *in = (const double *)in_base + off;
         double *out = (double *)out_base + off;
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(v, p->w, in, out, st);
+        if (algo == CS_ALGO_FP64_TC && fp64_tc1d_ok(p) && row0 == 0 && rows == p->view.ext[0] &&
+            reinterpret_cast<uintptr_t>(in_base) % 16 == 0 && reinterpret_cast<uintptr_t>(out_base) % 16 == 0)
+            return cs::launch_fp64_sweep_tc_rows1d(rows, p->w7, p->layout.origin, (const double *)in_base,
+                                                   (double *)out_base, p->wait, st);
         if (algo == CS_ALGO_FP64_TC && fp64_tc3d_ok(p) && cs::split_tc3d_layout_ok(v, off, in_base, out_base))
             return cs::launch_fp64_sweep_tc3d(v, p->w, off, p->layout.elements, (const double *)in_base,
                                               (double *)out_base, p->wait, st);
@@ -421,7 +440,7 @@ cs_status choose_algo(cs_plan *p, const void *a, void *b, cudaStream_t st, int *
         cand[nc++] = CS_ALGO_SPLIT_MMA_TMA;
         cand[nc++] = CS_ALGO_SPLIT_FMA;
     } else {
-        const bool tc = fp64_tc_ok(p) || fp64_tc3d_ok(p);
+        const bool tc = fp64_tc_ok(p) || fp64_tc3d_ok(p) || fp64_tc1d_ok(p);
         if ((p->algo == CS_ALGO_FP64_MMA && fp64_mma_ok(p)) || (p->algo == CS_ALGO_FP64_TC && tc)) {
             *out = p->algo;
             return CS_OK;
@@ -605,6 +624,10 @@ cudaError_t fp64_anchor_sweep_fp64_in(const cs_plan *p, const void *src, void *d
         return launch_fp64_sweep_tc(p->view, p->w7, off, n, (const double *)src, (double *)dst, p->wait, st);
     if (fp64_tc3d_geometry_ok(p) && split_tc3d_layout_ok(p->view, off, src, dst))
         return launch_fp64_sweep_tc3d(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
+    if (fp64_tc1d_geometry_ok(p) && reinterpret_cast<uintptr_t>(src) % 16 == 0 &&
+        reinterpret_cast<uintptr_t>(dst) % 16 == 0)
+        return launch_fp64_sweep_tc_rows1d(p->view.ext[0], p->w7, off, (const double *)src, (double *)dst, p->wait,
+                                           st);
     return launch_fp64_fma(p->view, p->radius, p->pattern, p->w, (const double *)src + off, (double *)dst + off, st);
 }
 
@@ -818,6 +841,8 @@ CS_API cs_status cs_plan_create(cs_plan **out, cs_shape shape, cs_semantics sem,
         const int k = 2 * p->radius + 1, o = 3 - p->radius;
         for (int i = 0; i < k; ++i)
             for (int j = 0; j < k; ++j) p->w7.v[(i + o) * 7 + j + o] = p->w.v[i * k + j];
+    } else if (p->dims == 1 && p->radius <= 3) {  // the taps in row 3 of the 7x7
+        for (int j = 0; j <= 2 * p->radius; ++j) p->w7.v[3 * 7 + 3 - p->radius + j] = p->w.v[j];
     }
     if (layout) {
         const cs_layout &L = *layout;
@@ -865,10 +890,11 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
             return fail(CS_ERR_INVALID_ARGUMENT, "FP64 algo needs an FP64 plan");
         if (v == CS_ALGO_FP64_MMA && !fp64_mma_ok(p))
             return fail(CS_ERR_UNSUPPORTED, "FP64 MMA serves 2D radius-3 dense FP64 plans only");
-        if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p) && !fp64_tc3d_ok(p))
+        if (v == CS_ALGO_FP64_TC && !fp64_tc_ok(p) && !fp64_tc3d_ok(p) && !fp64_tc1d_ok(p))
             return fail(CS_ERR_UNSUPPORTED,
                         "FP64 tcgen05 serves 2D FP64 plans of radius up to 3 and at least 8x8 on even-aligned "
-                        "layouts and 3D radius-1 FP64 plans");
+                        "layouts, 3D radius-1 FP64 plans and 1D FP64 plans of radius up to 3 whose length is a "
+                        "multiple of 64 (at least 512) with 4 points of halo");
         if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
             p->algo = (int)v;
             return CS_OK;

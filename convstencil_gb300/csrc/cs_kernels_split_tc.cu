@@ -225,7 +225,7 @@ template <class F, bool BATCH>
 __global__ void __launch_bounds__(kThreads<F>, 1)
     k2d_tc(const __grid_constant__ CUtensorMap tmap, typename F::Out *__restrict__ out, int m, int n,
            long long ld, int tiles_x, int tiles, int map_x, int map_y, typename F::Digits sw, WaitCfg wc,
-           const TcGrid<F> *__restrict__ grids, int ngrids)
+           const TcGrid<F> *__restrict__ grids, int ngrids, const void *__restrict__ line)
 {
     constexpr int D = F::kDigits;
     using SM = Smem<F>;
@@ -258,6 +258,22 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
             y0 = ty * TY;
         }
     };
+    // 1D row view: window rows r0, r0 + dr, .. of tile `it`; window row r is
+    // view row y0 - 3 + r, the 72 points from `line` + 64 (y0 - 3 + r). Rows
+    // before the first or after the last view row repeat that row: they meet
+    // zero weights, and a repeat of a row of the same tile leaves its scale
+    // and its non-finite test as they were.
+    auto load_rows = [&](int it, unsigned bar, int r0, int dr) {
+        int g, x0, y0;
+        tile_at(it, g, x0, y0);
+        const unsigned dst = smem_addr(S.stage);
+#pragma unroll 1
+        for (int r = r0; r < ST_Y; r += dr) {
+            const int vr = min(max(y0 - 3 + r, 0), m - 1);
+            bulk_load(dst + r * (ST_X * 8), static_cast<const char *>(line) + (long long)vr * (TX * 8), ST_X * 8,
+                      bar);
+        }
+    };
     auto load_window = [&](int it, unsigned bar) {
         int g, x0, y0;
         tile_at(it, g, x0, y0);
@@ -269,6 +285,12 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
             my = grids[g].map_y;
         }
         mbar_expect_tx(bar, kStageBytes);
+        if constexpr (!BATCH) {
+            if (line != nullptr) {
+                load_rows(it, bar, 0, 1);
+                return;
+            }
+        }
         tma_load_2d(smem_addr(S.stage), map, mx + x0 - 4, my + y0 - 3, bar);
     };
     volatile int *abort = &S.abort;
@@ -323,7 +345,23 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
 
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
-        if (lane == 0 && !wc.skip_loads) {
+        bool rows_1d = false;
+        if constexpr (!BATCH) rows_1d = line != nullptr;
+        if (rows_1d && !wc.skip_loads) {
+            // 70 row copies a tile: lane 0 waits for the stage and sets the
+            // byte count, then every lane issues rows lane, lane + 32, ..
+            for (int it = __shfl_sync(0xffffffffu, issued, 0); it < my_tiles; ++it) {
+                int ok = 1;
+                if (lane == 0) {
+                    ok = wait(stage_empty, (it & 1) ^ 1);
+                    if (ok) mbar_expect_tx(stage_full, kStageBytes);
+                }
+                if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                load_rows(it, stage_full, lane, 32);
+                issued = it + 1;
+            }
+        } else if (lane == 0 && !wc.skip_loads) {
             for (int it = issued; it < my_tiles; ++it) {
                 if (!wait(stage_empty, (it & 1) ^ 1)) break;
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -607,7 +645,7 @@ cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long 
     return launch_programmatic(k2d_tc<F, false>, grid, kThreads<F>, sizeof(Smem<F>) + 128, st, map,
                                reinterpret_cast<typename F::Out *>(out_base) + origin, (int)g.ext[0],
                                (int)g.ext[1], ld, tiles_x, tiles, (int)(origin % ld), (int)(origin / ld), digits,
-                               wc, static_cast<const TcGrid<F> *>(nullptr), 0);
+                               wc, static_cast<const TcGrid<F> *>(nullptr), 0, static_cast<const void *>(nullptr));
 }
 
 template <class F>
@@ -649,7 +687,8 @@ cudaError_t launch_batch(const void *records, int ngrids, int total, const WaitC
     // so the set-up may read them before pdl_wait().
     return launch_programmatic(k2d_tc<F, true>, grid, kThreads<F>, sizeof(Smem<F>) + 128, st, unused,
                                static_cast<typename F::Out *>(nullptr), 0, 0, 0LL, 0, total, 0, 0,
-                               typename F::Digits{}, wc, reinterpret_cast<const TcGrid<F> *>(records), ngrids);
+                               typename F::Digits{}, wc, reinterpret_cast<const TcGrid<F> *>(records), ngrids,
+                               static_cast<const void *>(nullptr));
 }
 
 split::SliceWeights split_digits(const Weights &w) { return split::slice_weights(w); }
@@ -670,6 +709,37 @@ cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long 
 {
     return launch_tc<FmtF64>(g, f64_slice_weights(w), origin, elements, in_base, out_base,
                              WaitCfg{wt.limit_ns, wt.skip_loads}, st);
+}
+
+cudaError_t launch_fp64_sweep_tc_rows1d(long long n, const Weights &w7, long long origin, const double *in_base,
+                                        double *out_base, const TcWait &wt, cudaStream_t st)
+{
+    // Row r of the view starts at point origin - 4 + 64 r and is 72 points
+    // wide: its outputs (columns 4..67) are the interior points
+    // origin + 64 r .. + 63, and columns 0..3 and 68..71 their neighbours on
+    // either side. The kernel sees an R x 64 grid (pitch 64) and copies each
+    // window row with its own bulk copy (rows of the view overlap, which a
+    // tensor map cannot describe); the taps sit in row 3 of the 7x7, so the
+    // window's other rows meet zero weights. Every copy reads 72 points at
+    // origin - 4 + 64 v (0 <= v < R): in bounds when the array holds 4 points
+    // of halo on either side, 16-byte aligned when the base is and origin is
+    // even.
+    if (n % TX != 0 || n < 8 * TX || origin < 4 || origin % 2 != 0 ||
+        reinterpret_cast<uintptr_t>(in_base) % 16 != 0 || reinterpret_cast<uintptr_t>(out_base) % 16 != 0)
+        return cudaErrorInvalidValue;
+    const long long rows = n / TX;
+    CUtensorMap unused;
+    std::memset(&unused, 0, sizeof unused);
+    cudaError_t e = set_smem_attr<FmtF64, false>();
+    if (e != cudaSuccess) return e;
+    const int tiles = (int)((rows + TY - 1) / TY);
+    const int grid = std::min(tiles, device_sm_count());
+    note_launch();
+    return launch_programmatic(k2d_tc<FmtF64, false>, grid, kThreads<FmtF64>, sizeof(Smem<FmtF64>) + 128, st,
+                               unused, out_base + origin, (int)rows, TX, (long long)TX, 1, tiles, 0, 0,
+                               f64_slice_weights(w7), WaitCfg{wt.limit_ns, wt.skip_loads},
+                               static_cast<const TcGrid<FmtF64> *>(nullptr), 0,
+                               static_cast<const void *>(in_base + origin - 4));
 }
 
 size_t tc_batch_record_bytes(bool fp64) { return fp64 ? sizeof(TcGrid<FmtF64>) : sizeof(TcGrid<FmtSplit>); }

@@ -344,6 +344,9 @@ cudaError_t encode_split_window_map_3d(CUtensorMap *map, const float2 *base, lon
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Rows of `width` 8-byte points that start `step` points apart (step <
+// width: consecutive rows overlap), `rows` of them: a 1D array seen as a 2D
+// grid whose rows carry their neighbours' points as halo. Box width x box_y.
 bool split_tma_layout_ok(const GridView &g, long long origin, const void *base)
 {
     if (g.dims != 2) return false;

@@ -104,7 +104,9 @@ typedef enum cs_algo {
                              centre of the 7x7) of at least 8x8, even pitch and interior column,
                              16-byte aligned buffers; also 3D radius-1 FP64
                              plans, box and star (an output's three plane parts are added as exact
-                             integers when their plane exponents agree, in FP64 otherwise) */
+                             integers when their plane exponents agree, in FP64 otherwise), and 1D
+                             FP64 plans of radius up to 3 whose length is a multiple of 64 (at
+                             least 512) with 4 halo points either side (as rows of 64 outputs) */
 } cs_algo;
 
 typedef enum cs_option {

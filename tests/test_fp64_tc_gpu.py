@@ -205,10 +205,70 @@ def test_fp64_tc_unsupported_plans_refuse_the_algorithm():
     with pytest.raises(cs.ConvStencilError) as e:
         tc_plan((4, 100), O.seeded_weights(49, 1))
     assert e.value.status == 2
-    p = cs.Plan("1d2r", (4096,), O.seeded_weights(5, 1))
+    p = cs.Plan("1d2r", (4100,), O.seeded_weights(5, 1))  # not a whole number of 64-point rows
     with pytest.raises(cs.ConvStencilError):
         p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
     ps = cs.Plan("box2d3r", (64, 64), O.seeded_weights(49, 1), precision=cs.Precision.SPLIT)
     with pytest.raises(cs.ConvStencilError) as e:
         ps.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
     assert e.value.status == 1
+
+
+
+@pytest.mark.parametrize("shape,taps,n,steps", [("1d1r", 3, 4096, 5), ("1d2r", 5, 8192, 4),
+                                                ("1d2r", 5, 512, 3), ("1d1r", 3, 64 * 4097, 2)])
+def test_fp64_tc_1d_plans(shape, taps, n, steps):
+    """1D plans on the 2D tcgen05 digit kernel: the array as rows of 64
+    outputs, each window row the 72 points around a row's outputs (taps in
+    row 3 of the 7x7, the other rows meeting zero weights)."""
+    w = O.seeded_weights(taps, 90 + n % 97)
+    p = cs.Plan(shape, (n,), w)
+    p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    x = O.splitmix_uniform(n, 91) - 0.5
+    buf = p.pack(x)
+    got = dev_run(p, buf, steps)
+    assert p.algo == cs.Algo.FP64_TC
+    L = p.layout.as_dict()
+    r = taps // 2
+    ref = O.run_1d(buf, w, r, n, L["origin"], steps)
+    err = rel_err(p.unpack(got), p.unpack(ref))
+    assert err[1] <= TOL, err  # normwise: signed data
+    halo = np.ones(p.elements, bool)
+    halo[p.interior_index().reshape(-1)] = False
+    assert not got[halo].any(), "halo must stay zero"
+    assert cs.device_wait_timeouts() == 0
+
+
+def test_fp64_tc_1d_fused_radius_three():
+    """Three fused 1d1r sweeps as one 7-point sweep (FUSED semantics)."""
+    n = 64 * 300
+    w7 = O.seeded_weights(7, 93)
+    p = cs.Plan("1d1r", (n,), w7, semantics=cs.Semantics.FUSED)
+    p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    x = O.splitmix_uniform(n, 94)
+    buf = p.pack(x)
+    got = dev_run(p, buf, 6)  # three steps per fused sweep
+    assert p.algo == cs.Algo.FP64_TC
+    ref = O.run_1d(buf, w7, 3, n, p.layout.as_dict()["origin"], 2)
+    assert rel_err(p.unpack(got), p.unpack(ref))[0] <= TOL
+
+
+def test_fp64_tc_1d_tuner_and_non_finite():
+    """AUTO may pick the 1D tcgen05 sweep; an Inf poisons the 64 x 64-output
+    tile whose window holds it (the window's rows are 64-point rows of the
+    array, so its neighbours within 3 rows of 64 points), not the others."""
+    n = 64 * 64 * 6
+    w = O.seeded_weights(5, 95)
+    p = cs.Plan("1d2r", (n,), w)
+    p.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    x = O.splitmix_uniform(n, 96)
+    x[64 * 100 + 5] = np.inf  # row 100 of the view: only tile 1's window (rows 61..130) holds it
+    got = p.unpack(dev_run(p, p.pack(x), 1))
+    assert p.algo == cs.Algo.FP64_TC
+    assert np.isnan(got[64 * 64:64 * 64 * 2]).all()
+    assert np.isfinite(got[:64 * 64]).all() and np.isfinite(got[64 * 64 * 2:]).all()
+    q = cs.Plan("1d2r", (n,), w)  # the tuner's pick, whichever it is, matches the oracle
+    y = O.splitmix_uniform(n, 97)
+    buf = q.pack(y)
+    ref = O.run_1d(buf, w, 2, n, q.layout.as_dict()["origin"], 3)
+    assert rel_err(q.unpack(dev_run(q, buf, 3)), q.unpack(ref))[0] <= TOL
