@@ -186,13 +186,14 @@ void native_layout(int dims, int r, const long long *ext, cs_layout &L)
     L.halo = r;
     const long long x0 = round_up(r, 2);  // interior rows start 16-byte aligned
     if (dims == 1) {
-        // at least 4 points of halo on either side: the 1D FP64 tcgen05 sweep
-        // reads rows of the array 4 points wider than their outputs each way
+        // at least 4 points of halo before the interior and 60 after it: the
+        // 1D FP64 tcgen05 sweep reads 4 neighbours either side of a row of 64
+        // outputs, as whole 64-point rows of the array from origin - 4
         const long long h1 = std::max(x0, 4LL);
         L.extent[0] = ext[0];
         L.pitch[0] = 1;
         L.origin = h1;
-        L.elements = round_up(h1 + ext[0] + std::max((long long)r, 4LL), 2);
+        L.elements = round_up(h1 + ext[0] + std::max((long long)r, 60LL), 2);
     } else if (dims == 2) {
         L.extent[0] = ext[0];
         L.extent[1] = ext[1];
@@ -324,13 +325,13 @@ bool fp64_tc3d_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc3
 
 // 1D plans of radius up to 3 on the 2D tcgen05 digit kernel through a row
 // view (launch_fp64_sweep_tc_rows1d): rows of 64 outputs, so the interior
-// must be a whole number of rows (at least 8), with an even origin and 4
-// points of halo on either side.
+// must be a whole number of rows (at least 8), with an even origin, 4 points
+// of halo before it and 60 points of the array after it.
 bool fp64_tc1d_geometry_ok(const cs_plan *p)
 {
     const long long n = p->view.ext[0], o = p->layout.origin;
     return p->dims == 1 && p->radius <= 3 && n % 64 == 0 && n >= 512 && o >= 4 && o % 2 == 0 &&
-           p->layout.elements >= o + n + 4;
+           p->layout.elements >= o + n + 60;
 }
 bool fp64_tc1d_ok(const cs_plan *p) { return p->prec == CS_PREC_FP64 && fp64_tc1d_geometry_ok(p); }
 
@@ -358,8 +359,8 @@ cudaError_t launch_sweep_rows(const cs_plan *p, int algo, const void *in_base, v
         if (algo == CS_ALGO_FP64_MMA) return cs::launch_fp64_mma_2d(v, p->w, in, out, st);
         if (algo == CS_ALGO_FP64_TC && fp64_tc1d_ok(p) && row0 == 0 && rows == p->view.ext[0] &&
             reinterpret_cast<uintptr_t>(in_base) % 16 == 0 && reinterpret_cast<uintptr_t>(out_base) % 16 == 0)
-            return cs::launch_fp64_sweep_tc_rows1d(rows, p->w7, p->layout.origin, (const double *)in_base,
-                                                   (double *)out_base, p->wait, st);
+            return cs::launch_fp64_sweep_tc_rows1d(rows, p->w7, p->layout.origin, p->layout.elements,
+                                                   (const double *)in_base, (double *)out_base, p->wait, st);
         if (algo == CS_ALGO_FP64_TC && fp64_tc3d_ok(p) && cs::split_tc3d_layout_ok(v, off, in_base, out_base))
             return cs::launch_fp64_sweep_tc3d(v, p->w, off, p->layout.elements, (const double *)in_base,
                                               (double *)out_base, p->wait, st);
@@ -626,8 +627,8 @@ cudaError_t fp64_anchor_sweep_fp64_in(const cs_plan *p, const void *src, void *d
         return launch_fp64_sweep_tc3d(p->view, p->w, off, n, (const double *)src, (double *)dst, p->wait, st);
     if (fp64_tc1d_geometry_ok(p) && reinterpret_cast<uintptr_t>(src) % 16 == 0 &&
         reinterpret_cast<uintptr_t>(dst) % 16 == 0)
-        return launch_fp64_sweep_tc_rows1d(p->view.ext[0], p->w7, off, (const double *)src, (double *)dst, p->wait,
-                                           st);
+        return launch_fp64_sweep_tc_rows1d(p->view.ext[0], p->w7, off, n, (const double *)src, (double *)dst,
+                                           p->wait, st);
     return launch_fp64_fma(p->view, p->radius, p->pattern, p->w, (const double *)src + off, (double *)dst + off, st);
 }
 
@@ -894,7 +895,7 @@ CS_API cs_status cs_plan_set_option(cs_plan *p, cs_option opt, long long v)
             return fail(CS_ERR_UNSUPPORTED,
                         "FP64 tcgen05 serves 2D FP64 plans of radius up to 3 and at least 8x8 on even-aligned "
                         "layouts, 3D radius-1 FP64 plans and 1D FP64 plans of radius up to 3 whose length is a "
-                        "multiple of 64 (at least 512) with 4 points of halo");
+                        "multiple of 64 (at least 512) with 4 points of halo before and 60 after the interior");
         if (v == CS_ALGO_SPLIT_TC && split_tc3d_ok(p)) {
             p->algo = (int)v;
             return CS_OK;

@@ -99,11 +99,12 @@ cudaError_t encode_split_window_map(CUtensorMap *map, const float2 *base, long l
                                     unsigned box_x, unsigned box_y);
 // 1D FP64 sweep of radius <= 3 on the 2D tcgen05 digit kernel: the n
 // interior points at `origin` (n a multiple of 64 and >= 512, origin even and
-// >= 4, at least 4 points of halo after them, 16-byte aligned bases) as rows
-// of 64 outputs, each read as the 72 points around them; w7 holds the taps in
-// row 3 of a 7x7.
-cudaError_t launch_fp64_sweep_tc_rows1d(long long n, const Weights &w7, long long origin, const double *in_base,
-                                        double *out_base, const TcWait &wait, cudaStream_t stream);
+// >= 4, at least 60 points of the array after them, 16-byte aligned bases) as
+// rows of 64 outputs, each read as the 72 points around them; w7 holds the
+// taps in row 3 of a 7x7.
+cudaError_t launch_fp64_sweep_tc_rows1d(long long n, const Weights &w7, long long origin, long long elements,
+                                        const double *in_base, double *out_base, const TcWait &wait,
+                                        cudaStream_t stream);
 // 3D tensor map: `planes` planes of pitch ldz, rows of pitch ld; box
 // box_x x box_y x 1.
 cudaError_t encode_split_window_map_3d(CUtensorMap *map, const float2 *base, long long ld, long long ldz,

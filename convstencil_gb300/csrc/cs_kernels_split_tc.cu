@@ -128,6 +128,10 @@ constexpr int NLV = 8 * R;                 // accumulator columns per level
 constexpr int kAccStride = 256;            // TMEM columns between the two accumulators
 constexpr int kTmemCols = 512;
 constexpr unsigned kStageBytes = ST_X * ST_Y * 8;  // 40,320 (8-byte points)
+// 1D row view: a tile's 70 window rows of 72 points lie in 71 array rows of 64
+constexpr int kSpanRows = ST_Y + 1;
+constexpr unsigned kSpanBytes = TX * kSpanRows * 8;  // 36,352
+static_assert(kSpanBytes <= kStageBytes, "the span fits the stage");
 constexpr int PAIRS = ST_X / 2, NPAIR = ST_Y * PAIRS;           // 36, 2,520
 constexpr int PER = (NPAIR + kSliceThreads - 1) / kSliceThreads;  // 10
 static_assert(FmtSplit::kEpiWarps == 4 && FmtF64::kEpiWarps == 8 && R == 4,
@@ -221,11 +225,11 @@ __device__ __forceinline__ int grid_of(const TcGrid<F> *grids, int ngrids, int t
 // each CTA takes a contiguous run of the batch's tiles, and the MMA warp
 // rebuilds its B matrices when the run crosses into the next grid, after
 // the MMAs of the previous tile have completed).
-template <class F, bool BATCH>
+template <class F, bool BATCH, bool ROWS1D = false>
 __global__ void __launch_bounds__(kThreads<F>, 1)
     k2d_tc(const __grid_constant__ CUtensorMap tmap, typename F::Out *__restrict__ out, int m, int n,
            long long ld, int tiles_x, int tiles, int map_x, int map_y, typename F::Digits sw, WaitCfg wc,
-           const TcGrid<F> *__restrict__ grids, int ngrids, const void *__restrict__ line)
+           const TcGrid<F> *__restrict__ grids, int ngrids)
 {
     constexpr int D = F::kDigits;
     using SM = Smem<F>;
@@ -258,22 +262,6 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
             y0 = ty * TY;
         }
     };
-    // 1D row view: window rows r0, r0 + dr, .. of tile `it`; window row r is
-    // view row y0 - 3 + r, the 72 points from `line` + 64 (y0 - 3 + r). Rows
-    // before the first or after the last view row repeat that row: they meet
-    // zero weights, and a repeat of a row of the same tile leaves its scale
-    // and its non-finite test as they were.
-    auto load_rows = [&](int it, unsigned bar, int r0, int dr) {
-        int g, x0, y0;
-        tile_at(it, g, x0, y0);
-        const unsigned dst = smem_addr(S.stage);
-#pragma unroll 1
-        for (int r = r0; r < ST_Y; r += dr) {
-            const int vr = min(max(y0 - 3 + r, 0), m - 1);
-            bulk_load(dst + r * (ST_X * 8), static_cast<const char *>(line) + (long long)vr * (TX * 8), ST_X * 8,
-                      bar);
-        }
-    };
     auto load_window = [&](int it, unsigned bar) {
         int g, x0, y0;
         tile_at(it, g, x0, y0);
@@ -284,13 +272,14 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
             mx = grids[g].map_x;
             my = grids[g].map_y;
         }
-        mbar_expect_tx(bar, kStageBytes);
-        if constexpr (!BATCH) {
-            if (line != nullptr) {
-                load_rows(it, bar, 0, 1);
-                return;
-            }
+        if constexpr (ROWS1D) {
+            // 1D row view: the span of 71 array rows of 64 points from view
+            // row y0 - 3 (rows outside the map read as zero)
+            mbar_expect_tx(bar, kSpanBytes);
+            tma_load_2d(smem_addr(S.stage), map, 0, y0 - 3, bar);
+            return;
         }
+        mbar_expect_tx(bar, kStageBytes);
         tma_load_2d(smem_addr(S.stage), map, mx + x0 - 4, my + y0 - 3, bar);
     };
     volatile int *abort = &S.abort;
@@ -345,23 +334,7 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
 
     if (warp == kWarpTma) {
         // ------------------------------------------------ TMA producer
-        bool rows_1d = false;
-        if constexpr (!BATCH) rows_1d = line != nullptr;
-        if (rows_1d && !wc.skip_loads) {
-            // 70 row copies a tile: lane 0 waits for the stage and sets the
-            // byte count, then every lane issues rows lane, lane + 32, ..
-            for (int it = __shfl_sync(0xffffffffu, issued, 0); it < my_tiles; ++it) {
-                int ok = 1;
-                if (lane == 0) {
-                    ok = wait(stage_empty, (it & 1) ^ 1);
-                    if (ok) mbar_expect_tx(stage_full, kStageBytes);
-                }
-                if (!__shfl_sync(0xffffffffu, ok, 0)) break;
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                load_rows(it, stage_full, lane, 32);
-                issued = it + 1;
-            }
-        } else if (lane == 0 && !wc.skip_loads) {
+        if (lane == 0 && !wc.skip_loads) {
             for (int it = issued; it < my_tiles; ++it) {
                 if (!wait(stage_empty, (it & 1) ^ 1)) break;
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -433,7 +406,12 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
                 const int idx = st + q * kSliceThreads;
                 v[q] = make_uint4(0u, 0u, 0u, 0u);
                 if (idx < NPAIR) {
-                    v[q] = S.stage[idx];
+                    // 1D row view: window row r (pairs 36 r ..) starts at pair
+                    // 32 r of the span, the 72 points from view row y0 - 3 + r
+                    if constexpr (ROWS1D)
+                        v[q] = S.stage[idx - 4 * (idx / PAIRS)];
+                    else
+                        v[q] = S.stage[idx];
                     if constexpr (F::kF64)
                         emax = max(emax, max((v[q].y >> 20) & 0x7FFu, (v[q].w >> 20) & 0x7FFu));
                     else
@@ -617,11 +595,11 @@ __global__ void __launch_bounds__(kThreads<F>, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-template <class F, bool BATCH>
+template <class F, bool BATCH, bool ROWS1D = false>
 cudaError_t set_smem_attr()
 {
-    static const cudaError_t err = cudaFuncSetAttribute(k2d_tc<F, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        (int)(sizeof(Smem<F>) + 128));
+    static const cudaError_t err = cudaFuncSetAttribute(
+        k2d_tc<F, BATCH, ROWS1D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(Smem<F>) + 128));
     return err;
 }
 
@@ -645,7 +623,7 @@ cudaError_t launch_tc(const GridView &g, const typename F::Digits &digits, long 
     return launch_programmatic(k2d_tc<F, false>, grid, kThreads<F>, sizeof(Smem<F>) + 128, st, map,
                                reinterpret_cast<typename F::Out *>(out_base) + origin, (int)g.ext[0],
                                (int)g.ext[1], ld, tiles_x, tiles, (int)(origin % ld), (int)(origin / ld), digits,
-                               wc, static_cast<const TcGrid<F> *>(nullptr), 0, static_cast<const void *>(nullptr));
+                               wc, static_cast<const TcGrid<F> *>(nullptr), 0);
 }
 
 template <class F>
@@ -687,8 +665,7 @@ cudaError_t launch_batch(const void *records, int ngrids, int total, const WaitC
     // so the set-up may read them before pdl_wait().
     return launch_programmatic(k2d_tc<F, true>, grid, kThreads<F>, sizeof(Smem<F>) + 128, st, unused,
                                static_cast<typename F::Out *>(nullptr), 0, 0, 0LL, 0, total, 0, 0,
-                               typename F::Digits{}, wc, reinterpret_cast<const TcGrid<F> *>(records), ngrids,
-                               static_cast<const void *>(nullptr));
+                               typename F::Digits{}, wc, reinterpret_cast<const TcGrid<F> *>(records), ngrids);
 }
 
 split::SliceWeights split_digits(const Weights &w) { return split::slice_weights(w); }
@@ -711,35 +688,36 @@ cudaError_t launch_fp64_sweep_tc(const GridView &g, const Weights &w, long long 
                              WaitCfg{wt.limit_ns, wt.skip_loads}, st);
 }
 
-cudaError_t launch_fp64_sweep_tc_rows1d(long long n, const Weights &w7, long long origin, const double *in_base,
-                                        double *out_base, const TcWait &wt, cudaStream_t st)
+cudaError_t launch_fp64_sweep_tc_rows1d(long long n, const Weights &w7, long long origin, long long elements,
+                                        const double *in_base, double *out_base, const TcWait &wt, cudaStream_t st)
 {
     // Row r of the view starts at point origin - 4 + 64 r and is 72 points
     // wide: its outputs (columns 4..67) are the interior points
     // origin + 64 r .. + 63, and columns 0..3 and 68..71 their neighbours on
-    // either side. The kernel sees an R x 64 grid (pitch 64) and copies each
-    // window row with its own bulk copy (rows of the view overlap, which a
-    // tensor map cannot describe); the taps sit in row 3 of the 7x7, so the
-    // window's other rows meet zero weights. Every copy reads 72 points at
-    // origin - 4 + 64 v (0 <= v < R): in bounds when the array holds 4 points
-    // of halo on either side, 16-byte aligned when the base is and origin is
-    // even.
-    if (n % TX != 0 || n < 8 * TX || origin < 4 || origin % 2 != 0 ||
+    // either side. The kernel sees an R x 64 grid (pitch 64); rows of the view
+    // overlap by 8 points, which a tensor map cannot describe, so a tile loads
+    // the span of 71 array rows of 64 points (from origin - 4, not
+    // overlapping) that holds its 70 window rows, and the slicers read window
+    // row r at point 64 r of the span. The taps sit in row 3 of the 7x7, so
+    // the window's other rows meet zero weights. The last tile's span reaches
+    // array row R (points origin + n - 4 .. origin + n + 59), so the array
+    // holds 60 points after the interior; the map covers its whole rows.
+    if (n % TX != 0 || n < 8 * TX || origin < 4 || origin % 2 != 0 || elements < origin + n + 60 ||
         reinterpret_cast<uintptr_t>(in_base) % 16 != 0 || reinterpret_cast<uintptr_t>(out_base) % 16 != 0)
         return cudaErrorInvalidValue;
     const long long rows = n / TX;
-    CUtensorMap unused;
-    std::memset(&unused, 0, sizeof unused);
-    cudaError_t e = set_smem_attr<FmtF64, false>();
+    CUtensorMap map;
+    cudaError_t e = encode_split_window_map(&map, reinterpret_cast<const float2 *>(in_base + origin - 4), TX,
+                                            (elements - (origin - 4)) / TX, TX, kSpanRows);
     if (e != cudaSuccess) return e;
+    if ((e = set_smem_attr<FmtF64, false, true>()) != cudaSuccess) return e;
     const int tiles = (int)((rows + TY - 1) / TY);
     const int grid = std::min(tiles, device_sm_count());
     note_launch();
-    return launch_programmatic(k2d_tc<FmtF64, false>, grid, kThreads<FmtF64>, sizeof(Smem<FmtF64>) + 128, st,
-                               unused, out_base + origin, (int)rows, TX, (long long)TX, 1, tiles, 0, 0,
+    return launch_programmatic(k2d_tc<FmtF64, false, true>, grid, kThreads<FmtF64>, sizeof(Smem<FmtF64>) + 128, st,
+                               map, out_base + origin, (int)rows, TX, (long long)TX, 1, tiles, 0, 0,
                                f64_slice_weights(w7), WaitCfg{wt.limit_ns, wt.skip_loads},
-                               static_cast<const TcGrid<FmtF64> *>(nullptr), 0,
-                               static_cast<const void *>(in_base + origin - 4));
+                               static_cast<const TcGrid<FmtF64> *>(nullptr), 0);
 }
 
 size_t tc_batch_record_bytes(bool fp64) { return fp64 ? sizeof(TcGrid<FmtF64>) : sizeof(TcGrid<FmtSplit>); }

@@ -197,16 +197,6 @@ __device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map
         : "memory");
 }
 
-// Untiled bulk copy of `bytes` from global to shared memory, completing on
-// `bar`: both addresses 16-byte aligned, bytes a multiple of 16.
-__device__ __forceinline__ void bulk_load(unsigned dst, const void *src, unsigned bytes, unsigned bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
-}
-
 __device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *map, int x, int y, int z,
                                             unsigned bar)
 {

@@ -92,6 +92,22 @@ def test_plan_validation_without_gpu():
                 precision=cs.Precision.SPLIT).set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
     with pytest.raises(cs.ConvStencilError):   # split algorithms need a split plan
         cs.Plan("box3d1r", (8, 8, 8), np.full(27, 1 / 27)).set_option(cs.Option.ALGO, cs.Algo.SPLIT_TC)
+    # 1D FP64 plans of radius <= 3 run on tcgen05 as rows of 64 outputs: the
+    # native layout keeps 4 points before the interior and 60 after it
+    p1 = cs.Plan("1d2r", (4096,), np.full(5, 0.2))
+    L1 = p1.layout.as_dict()
+    assert L1["origin"] >= 4 and L1["origin"] % 2 == 0 and L1["elements"] >= L1["origin"] + 4096 + 60
+    p1.set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    cs.Plan("1d1r", (512,), np.full(7, 1 / 7), semantics=cs.Semantics.FUSED).set_option(cs.Option.ALGO,
+                                                                                         cs.Algo.FP64_TC)
+    for ext, kw in (((4100,), {}), ((448,), {}),  # not whole 64-point rows / fewer than 8 rows
+                    ((4096,), {"layout": {"dims": 1, "halo": 4, "extent": [4096], "pitch": [1], "origin": 4,
+                                          "elements": 4104}})):  # no 60-point tail
+        with pytest.raises(cs.ConvStencilError):
+            cs.Plan("1d2r", ext, np.full(5, 0.2), **kw).set_option(cs.Option.ALGO, cs.Algo.FP64_TC)
+    with pytest.raises(cs.ConvStencilError):   # fused 1d2r is radius 4
+        cs.Plan("1d2r", (4096,), np.full(9, 1 / 9), semantics=cs.Semantics.FUSED).set_option(
+            cs.Option.ALGO, cs.Algo.FP64_TC)
 
 
 def test_pack_unpack_roundtrip():
