@@ -460,7 +460,8 @@ def run_pipe_peaks():
 # ------------------------------------------------------------ ncu cases
 def run_kernel_case(args):
     """One box2d3r plan (box3d1r on an h x m x n grid for split_tc3d and
-    fp64_tc3d), one algorithm, `sweeps` sweeps on an m x n grid."""
+    fp64_tc3d; 1d2r on m x n points for fp64_tc_rows1d and fp64_fma_1d), one
+    algorithm, `sweeps` sweeps on an m x n grid."""
     import torch
     import convstencil_gb300 as cs
     from convstencil_gb300 import workload as WL
@@ -468,12 +469,15 @@ def run_kernel_case(args):
     shape, ext, taps = SHAPE, (m, n), TAPS
     if args.kernel_case in ("split_tc3d", "fp64_tc3d"):
         shape, ext, taps = "box3d1r", (args.h, m, n), 27
+    if args.kernel_case in ("fp64_tc_rows1d", "fp64_fma_1d"):
+        shape, ext, taps = "1d2r", (m * n,), 5
     x = WL.splitmix_uniform(int(np.prod(ext)), GRID_SEED).reshape(ext)
     w = WL.seeded_weights(taps, WEIGHT_SEED)
     algo = {"fp64_fma": cs.Algo.FP64_FMA, "fp64_mma": cs.Algo.FP64_MMA, "fp64_tc": cs.Algo.FP64_TC,
             "split_mma": cs.Algo.SPLIT_MMA, "split_mma_tma": cs.Algo.SPLIT_MMA_TMA,
             "split_fma": cs.Algo.SPLIT_FMA, "split_tc": cs.Algo.SPLIT_TC,
-            "split_tc3d": cs.Algo.SPLIT_TC, "fp64_tc3d": cs.Algo.FP64_TC}[args.kernel_case]
+            "split_tc3d": cs.Algo.SPLIT_TC, "fp64_tc3d": cs.Algo.FP64_TC,
+            "fp64_tc_rows1d": cs.Algo.FP64_TC, "fp64_fma_1d": cs.Algo.FP64_FMA}[args.kernel_case]
     split = args.kernel_case.startswith("split")
     p = cs.Plan(shape, ext, w, precision=cs.Precision.SPLIT if split else cs.Precision.FP64)
     p.set_option(cs.Option.ALGO, algo)
@@ -587,9 +591,10 @@ def main():
                          "saturated comparison, print their line and exit")
     ap.add_argument("--kernel-case", default=None,
                     choices=["fp64_fma", "fp64_mma", "fp64_tc", "split_mma", "split_mma_tma", "split_fma",
-                             "split_tc", "split_tc3d", "fp64_tc3d"],
+                             "split_tc", "split_tc3d", "fp64_tc3d", "fp64_tc_rows1d", "fp64_fma_1d"],
                     help="run one box2d3r kernel for --sweeps sweeps on an --m x --n grid (split_tc3d, "
-                         "fp64_tc3d: box3d1r on --h x --m x --n) (small cases for ncu captures) and exit")
+                         "fp64_tc3d: box3d1r on --h x --m x --n; fp64_tc_rows1d, fp64_fma_1d: 1d2r on "
+                         "--m * --n points) (small cases for ncu captures) and exit")
     ap.add_argument("--m", type=int, default=4608)
     ap.add_argument("--n", type=int, default=4608)
     ap.add_argument("--h", type=int, default=256)
