@@ -151,7 +151,8 @@ typedef struct cs_plan cs_plan;
 
 /* extent: `dims` interior sizes, slowest first. weights: see cs_semantics.
  * layout: NULL for the library's native layout (rows padded to 16 bytes,
- * halo = the sweep's radius), or the caller's own layout. */
+ * halo = the sweep's radius; 1D: at least 4 points before the interior and
+ * 60 after it), or the caller's own layout. */
 CS_API cs_status cs_plan_create(cs_plan **plan, cs_shape shape, cs_semantics sem,
                                 cs_precision prec, const long long *extent,
                                 const double *weights, int n_weights,
