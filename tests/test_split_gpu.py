@@ -124,12 +124,14 @@ def test_split_signed_weights_and_wide_range():
 
 @pytest.mark.parametrize("shape,ext,algo", [("box2d3r", (256, 320), cs.Algo.SPLIT_TC),
                                              ("box3d1r", (64, 64, 72), cs.Algo.SPLIT_TC),
-                                             ("box3d1r", (40, 48, 56), cs.Algo.SPLIT_FMA)])
+                                             ("box3d1r", (40, 48, 56), cs.Algo.SPLIT_FMA),
+                                             ("1d2r", (4096,), cs.Algo.SPLIT_FMA)])
 def test_split_long_run_with_fp64_reanchor(shape, ext, algo):
     """200 steps with and without FP64 re-anchor sweeps (one sweep in every
-    100 computed in FP64 from the (hi, lo) state): both within the 1e-10
-    pointwise bar against the oracle, and the re-anchored run differs from
-    the plain one (the FP64 sweeps really run)."""
+    100 computed in FP64 from the (hi, lo) state; the 1D plan's on the FP64
+    tcgen05 rows): both within the 1e-10 pointwise bar against the oracle,
+    and the re-anchored run differs from the plain one (the FP64 sweeps
+    really run)."""
     info = cs.SHAPE_INFO[cs.SHAPE_BY_NAME[shape]]
     w = O.seeded_weights(info[1], 21)
     x = O.splitmix_uniform(int(np.prod(ext)), 22).reshape(ext)
