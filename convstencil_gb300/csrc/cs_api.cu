@@ -851,9 +851,20 @@ CS_API cs_status cs_plan_create(cs_plan **out, cs_shape shape, cs_semantics sem,
         for (int d = 0; ok && d < si.dims; ++d) ok = L.extent[d] == extent[d] && L.pitch[d] >= 1;
         if (ok && si.dims >= 2) ok = L.pitch[si.dims - 2] >= L.extent[si.dims - 1] + 2 * p->radius;
         if (ok && si.dims == 3) ok = L.pitch[0] >= L.pitch[1] * (L.extent[1] + 2 * p->radius);
+        if (ok) {
+            // every point within the radius of the interior (the box around
+            // it) lies in the buffer: the kernels read all of them
+            __int128 lo = L.origin, hi = L.origin;
+            for (int d = 0; d < si.dims; ++d) {
+                lo -= (__int128)p->radius * L.pitch[d];
+                hi += (__int128)(L.extent[d] - 1 + p->radius) * L.pitch[d];
+            }
+            ok = lo >= 0 && hi < (__int128)L.elements;
+        }
         if (!ok) {
+            const int r = p->radius;
             delete p;
-            return fail(CS_ERR_INVALID_ARGUMENT, "layout does not fit the grid with halo %d", p->radius);
+            return fail(CS_ERR_INVALID_ARGUMENT, "layout does not fit the grid with halo %d", r);
         }
         p->layout = L;
         p->layout.bytes = (size_t)L.elements * sizeof(double);
@@ -869,9 +880,10 @@ CS_API cs_status cs_plan_create(cs_plan **out, cs_shape shape, cs_semantics sem,
                                ? cs::fp64_fma_supported(p->dims, p->radius, p->pattern)
                                : cs::split_supported(p->dims, p->radius, p->pattern);
     if (!supported) {
+        const int r = p->radius, pat = p->pattern;
         delete p;
-        return fail(CS_ERR_UNSUPPORTED, "no kernel for dims=%d radius=%d pattern=%d precision=%d",
-                    si.dims, p->radius, p->pattern, (int)prec);
+        return fail(CS_ERR_UNSUPPORTED, "no kernel for dims=%d radius=%d pattern=%d precision=%d", si.dims, r, pat,
+                    (int)prec);
     }
     *out = p;
     return CS_OK;

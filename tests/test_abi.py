@@ -80,6 +80,17 @@ def test_plan_validation_without_gpu():
         cs.Plan("box2d3r", (8, 8), np.ones(49), layout={"dims": 2, "halo": 1, "extent": [8, 8],
                                                         "pitch": [10, 1], "origin": 11,
                                                         "elements": 100})
+    for origin, elements in ((3 * 14 + 4, 13 * 14), (2 * 14 + 4, 14 * 14), (14 * 3 + 2, 14 * 14)):
+        # box2d3r 8x8 with pitch 14: a buffer too short for the last halo
+        # rows, an origin 2 rows down (the first halo row before the buffer),
+        # an origin 2 columns in (the halo's first column in the row before)
+        with pytest.raises(cs.ConvStencilError) as e:
+            cs.Plan("box2d3r", (8, 8), np.ones(49), layout={"dims": 2, "halo": 3, "extent": [8, 8],
+                                                            "pitch": [14, 1], "origin": origin,
+                                                            "elements": elements})
+        assert e.value.status == 1 and "halo 3" in str(e.value)
+    cs.Plan("box2d3r", (8, 8), np.ones(49), layout={"dims": 2, "halo": 3, "extent": [8, 8], "pitch": [14, 1],
+                                                    "origin": 3 * 14 + 3, "elements": 14 * 14})  # fits exactly
     with pytest.raises(cs.ConvStencilError):   # MMA algo only for FP64 2D radius-3 dense
         cs.Plan("star2d1r", (8, 8), np.ones(5)).set_option(cs.Option.ALGO, cs.Algo.FP64_MMA)
     # tcgen05: split plans of 2D radius 3 and of 3D radius 1 (27 weights)
